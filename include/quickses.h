@@ -1,0 +1,176 @@
+/*
+ * quickses_gb300 - GB300-native SES mesher, drop-in for QuickSES's library path.
+ *
+ * Two layers of entry points live in libquickses_gb300.so:
+ *
+ *  1. The QuickSES library surface, with the same symbol names, signatures and
+ *     semantics as the reference (CudaSurf.h:75-83, CudaSurf.cu:778-873).  These are thin
+ *     wrappers over a process-wide default context and are, like the reference, not
+ *     reentrant.
+ *  2. Reentrant qses_* calls: a context per caller thread/stream, explicit parameters
+ *     (voxel size, smoothing passes, slice), status codes instead of exit(), and meshes
+ *     owned by the caller until qses_mesh_release.
+ *
+ * All pointers are host pointers unless a name says "device".  No CUDA or torch types
+ * appear in the signatures: qses_float3 has the layout of CUDA's float3 (3 packed floats).
+ */
+#ifndef QUICKSES_GB300_H
+#define QUICKSES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef QSES_API
+#define QSES_API
+#endif
+
+typedef struct { float x, y, z; } qses_float3;
+
+#ifdef __cplusplus
+#define QSES_BOOL bool
+#else
+#define QSES_BOOL _Bool
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+enum {
+    QSES_OK = 0,
+    QSES_ERR_INVALID_ARG = 1,   /* bad pointer / size / parameter */
+    QSES_ERR_NO_DEVICE = 2,     /* no CUDA device, or not an sm_103 device */
+    QSES_ERR_CUDA = 3,          /* a CUDA runtime call failed */
+    QSES_ERR_OUT_OF_MEMORY = 4, /* device or pinned host allocation failed */
+    QSES_ERR_UNSUPPORTED = 5,   /* input outside the supported envelope (see qses_status_string) */
+    QSES_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up */
+    QSES_ERR_INTERNAL = 7       /* internal consistency check failed */
+};
+
+/* --------------------------------------------- QuickSES-compatible library surface */
+
+/* Replaces API_computeSES (CudaSurf.h:77-78, CudaSurf.cu:787-841).  Inputs are read
+ * only.  out_vertices and out_triangles are ignored, as in the reference; *NVert is the
+ * vertex count and *NTri the number of triangle INDICES (3 x kept triangles).  Results
+ * stay in library-owned buffers reachable through API_get*.  Triangles with a repeated
+ * vertex index are dropped.  doSmoothing = number of Laplacian passes.  N <= 1 gives an
+ * empty mesh.  Unlike the reference, a failure does not exit(): counts are left at 0 and
+ * qses_api_last_status() reports the code. */
+QSES_API void API_computeSES(float resoSES, qses_float3 *atomPos, float *atomRad, unsigned int N,
+                             qses_float3 *out_vertices, unsigned int *NVert, int *out_triangles,
+                             unsigned int *NTri, int doSmoothing);
+/* Replaces API_getTriangles (CudaSurf.h:79, CudaSurf.cu:845-857): when invertTriangles
+ * is true the first two indices of every triangle are swapped in place (calling twice
+ * toggles back).  C callers pass 0/1 in a single byte, as C++ bool. */
+QSES_API int *API_getTriangles(QSES_BOOL invertTriangles);
+/* Replaces API_getVertices (CudaSurf.h:80, CudaSurf.cu:858-861). */
+QSES_API qses_float3 *API_getVertices(void);
+/* Replaces API_freeMesh (CudaSurf.h:81, CudaSurf.cu:867-872). */
+QSES_API void API_freeMesh(void);
+/* Replaces API_getAtomIdPerVert (CudaSurf.h:82, CudaSurf.cu:862-865): index of the
+ * closest atom in the cell-sorted atom order, as the reference returns it. */
+QSES_API int *API_getAtomIdPerVert(void);
+
+/* Exported data symbols of the reference library (CudaSurf.cu:778-785). */
+extern QSES_API int NTriangles;
+extern QSES_API int NVertices;
+extern QSES_API int *globalTriangles;
+extern QSES_API qses_float3 *globalVertices;
+extern QSES_API int *globalIdAtomPerVert;
+
+/* Status of the last API_computeSES call (no reference counterpart: the reference
+ * exits the process on error, CudaSurf.h:54-62). */
+QSES_API int qses_api_last_status(void);
+
+/* ------------------------------------------------------------ reentrant interface */
+
+typedef struct qses_context qses_context;
+
+typedef struct {
+    float voxel;        /* SES voxel size in A (CLI -v, default 0.5) */
+    int smooth_passes;  /* Laplacian passes (CLI -l, default 1) */
+    int slice;          /* CLI -s: x-slab thickness in voxels for the field (memory
+                           schedule only; the mesh does not depend on it), default 300 */
+    int flags;          /* QSES_FLAG_* */
+} qses_params;
+
+#define QSES_FLAG_KEEP_DEGENERATE 1  /* keep triangles with a repeated index (CLI/OBJ path) */
+
+typedef struct {
+    unsigned n_vertices;
+    unsigned n_triangles;      /* triangles (not indices) */
+    qses_float3 *vertices;     /* smoothed welded vertices, lexicographic order of the
+                                  quantised position */
+    int *triangles;            /* 3 * n_triangles vertex indices */
+    int *atom_sorted;          /* closest atom, index into the cell-sorted atom order */
+    int *atom_input;           /* closest atom, index into the caller's atom array */
+    int grid_dim;              /* SES grid voxels per axis */
+    float origin[3];           /* grid origin (A) */
+    void *_owner;              /* release with qses_mesh_release */
+} qses_mesh;
+
+/* Creates a context on CUDA device `device`; `cuda_stream` is a cudaStream_t to run on,
+ * or NULL for a private non-blocking stream.  Fails with QSES_ERR_NO_DEVICE without a
+ * usable sm_103 GPU. */
+QSES_API int qses_context_create(int device, void *cuda_stream, qses_context **out);
+QSES_API int qses_context_destroy(qses_context *ctx);
+QSES_API void qses_params_default(qses_params *p);
+
+/* Host atoms in, host mesh out (pinned, owned by *out until qses_mesh_release). */
+QSES_API int qses_compute(qses_context *ctx, const qses_params *p, const qses_float3 *atoms,
+                          const float *radii, unsigned n, qses_mesh *out);
+QSES_API void qses_mesh_release(qses_mesh *m);
+
+/* Device-resident form: atoms already in device memory (3n floats, n floats); the mesh
+ * stays on the device in the context's workspace (valid until the next call on `ctx`).
+ * Counts are returned on the host. */
+typedef struct {
+    unsigned n_vertices, n_triangles;
+    float *d_vertices;   /* 3 * n_vertices */
+    int *d_triangles;    /* 3 * n_triangles */
+    int *d_atom_sorted;
+    int *d_atom_input;
+} qses_device_mesh;
+QSES_API int qses_compute_device(qses_context *ctx, const qses_params *p, const float *d_xyz,
+                                 const float *d_radii, unsigned n, qses_device_mesh *out);
+
+QSES_API const char *qses_status_string(int status);
+QSES_API const char *qses_last_error(qses_context *ctx);
+
+/* Per-stage device times (ms, CUDA events on the context stream) of the last call when
+ * profiling is on.  Returns the number of stages written. */
+QSES_API int qses_set_profiling(qses_context *ctx, int on);
+QSES_API int qses_stage_times(qses_context *ctx, float *ms, const char **names, int max);
+/* Number of kernels the last call launched. */
+QSES_API int qses_last_launch_count(qses_context *ctx);
+
+/* --------------------------------------------------- inspection (tests, tooling) */
+
+typedef struct {
+    float origin[3], cell, dx, probe, max_radius, max_dist;
+    int gnb, G, R, Gc, W;
+} qses_grid_info;
+
+/* Grid sizing exactly as the reference computes it (CudaSurf.cu:149-174, 250-253,
+ * 546-574, 629-635); host-only. */
+QSES_API int qses_grid_info_for(const qses_float3 *atoms, const float *radii, unsigned n, float voxel,
+                                qses_grid_info *out);
+/* Voxel codes of the last qses_compute on ctx (G*G*G bytes, x-major, z fastest): n<=3R^2 =
+ * squared voxel distance to the nearest outside voxel, 253 none in window, 254 inside,
+ * 255 outside. */
+QSES_API int qses_debug_codes(qses_context *ctx, uint8_t *codes, size_t bytes);
+/* Cell-sorted atom order of the last call: sorted_to_input[n], cell hash per sorted atom. */
+QSES_API int qses_debug_atom_order(qses_context *ctx, uint32_t *sorted_to_input, uint32_t *hash, unsigned n);
+
+/* --------------------------------------------------------- synthetic molecules */
+QSES_API int qses_synth_ball(unsigned N, uint64_t seed, float density, float min_dist, float *xyz,
+                             float *rad, unsigned char *elem);
+QSES_API int qses_synth_shell(unsigned N, uint64_t seed, float r_in, float thickness, float min_dist,
+                              float *xyz, float *rad, unsigned char *elem);
+QSES_API int qses_synth_jitter(const float *base_xyz, unsigned N, float sigma, uint64_t seed, float *out_xyz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QUICKSES_GB300_H */

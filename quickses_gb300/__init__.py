@@ -1,0 +1,9 @@
+"""GB300-native SES mesher: a drop-in for QuickSES's atoms+radii -> SES mesh path.
+
+The compute path is libquickses_gb300.so (hand-written sm_103a CUDA behind a C-ABI that
+exports QuickSES's API_* symbols); this package is its Python face.
+"""
+from .api import Context, Mesh, QSESError, ReferenceAPI, compute_ses, grid_info  # noqa: F401
+from . import molecules  # noqa: F401
+
+__all__ = ["Context", "Mesh", "QSESError", "ReferenceAPI", "compute_ses", "grid_info", "molecules"]

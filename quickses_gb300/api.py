@@ -1,0 +1,207 @@
+"""Python face of the SES mesher, mirroring QuickSES's library path.
+
+QuickSES's entry point is ``API_computeSES(reso, atomPos, atomRad, N, ...)`` followed by
+``API_getVertices / API_getTriangles / API_getAtomIdPerVert / API_freeMesh``
+(CudaSurf.cu:787-873).  :func:`compute_ses` is the same call through a reentrant context;
+:class:`ReferenceAPI` exposes the ``API_*`` symbols unchanged for callers that want the
+exact reference semantics (index count in ``NTri``, sorted atom ids, in-place winding
+swap).  Everything runs on the GPU through libquickses_gb300.so; there is no CPU path.
+"""
+import ctypes
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+
+
+class QSESError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__("%s (status %d)" % (message, code))
+        self.code = code
+
+
+@dataclass
+class Mesh:
+    vertices: np.ndarray      # (nv, 3) float32, smoothed
+    triangles: np.ndarray     # (nt, 3) int32
+    atom_sorted: np.ndarray   # (nv,) int32 closest atom in the cell-sorted order (reference ids)
+    atom_input: np.ndarray    # (nv,) int32 closest atom in the caller's order
+    grid_dim: int
+    origin: tuple
+
+
+def _f32(a, shape_last=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape_last is not None and (a.ndim != 2 or a.shape[1] != shape_last):
+        raise ValueError("expected an (N, %d) array" % shape_last)
+    return a
+
+
+class Context:
+    """One CUDA stream and its reusable device workspace (qses_context)."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None):
+        self._lib = L.lib()
+        h = ctypes.c_void_p()
+        rc = self._lib.qses_context_create(device, ctypes.c_void_p(stream) if stream else None, ctypes.byref(h))
+        if rc != L.QSES_OK:
+            raise QSESError(rc, "qses_context_create: " + L.status_string(rc))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.qses_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _params(self, voxel, smooth, keep_degenerate, slice_):
+        p = L.Params()
+        self._lib.qses_params_default(ctypes.byref(p))
+        p.voxel = float(voxel)
+        p.smooth_passes = int(smooth)
+        p.slice = int(slice_)
+        p.flags = L.QSES_FLAG_KEEP_DEGENERATE if keep_degenerate else 0
+        return p
+
+    def _check(self, rc, what):
+        if rc != L.QSES_OK:
+            raise QSESError(rc, "%s: %s" % (what, self._lib.qses_last_error(self._h).decode()))
+
+    def compute(self, xyz, radii, voxel=0.5, smooth=1, keep_degenerate=False, slice=300) -> Mesh:
+        """Atoms (N, 3) + radii (N,) on the host -> welded, smoothed mesh on the host."""
+        xyz = _f32(xyz, 3)
+        radii = _f32(radii)
+        if radii.shape != (xyz.shape[0],):
+            raise ValueError("radii must have shape (N,)")
+        m = L.Mesh()
+        rc = self._lib.qses_compute(self._h, ctypes.byref(self._params(voxel, smooth, keep_degenerate, slice)),
+                                    xyz.ctypes.data_as(ctypes.c_void_p),
+                                    radii.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), xyz.shape[0],
+                                    ctypes.byref(m))
+        self._check(rc, "qses_compute")
+        try:
+            nv, nt = m.n_vertices, m.n_triangles
+
+            def take(ptr, n, dt, shape):
+                if n == 0:
+                    return np.zeros(shape, dt)
+                return np.ctypeslib.as_array(ptr, shape=(n * (shape[1] if len(shape) > 1 else 1),)).astype(
+                    dt, copy=True).reshape(shape)
+
+            out = Mesh(take(m.vertices, nv, np.float32, (nv, 3)), take(m.triangles, nt, np.int32, (nt, 3)),
+                       take(m.atom_sorted, nv, np.int32, (nv,)), take(m.atom_input, nv, np.int32, (nv,)),
+                       int(m.grid_dim), tuple(m.origin))
+        finally:
+            self._lib.qses_mesh_release(ctypes.byref(m))
+        return out
+
+    def compute_device(self, d_xyz_ptr, d_radii_ptr, n, voxel=0.5, smooth=1, keep_degenerate=False):
+        """Device-resident form (pointers to device float arrays); returns counts and the
+        device pointers of the mesh, valid until the next call on this context."""
+        dm = L.DeviceMesh()
+        rc = self._lib.qses_compute_device(self._h, ctypes.byref(self._params(voxel, smooth, keep_degenerate, 300)),
+                                           ctypes.c_void_p(d_xyz_ptr), ctypes.c_void_p(d_radii_ptr), n,
+                                           ctypes.byref(dm))
+        self._check(rc, "qses_compute_device")
+        return dm
+
+    def debug_codes(self, G):
+        codes = np.zeros((G, G, G), np.uint8)
+        rc = self._lib.qses_debug_codes(self._h, codes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), codes.nbytes)
+        self._check(rc, "qses_debug_codes")
+        return codes
+
+    def debug_atom_order(self, n):
+        order = np.zeros(n, np.uint32)
+        keys = np.zeros(n, np.uint32)
+        rc = self._lib.qses_debug_atom_order(self._h, order.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                             keys.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), n)
+        self._check(rc, "qses_debug_atom_order")
+        return order, keys
+
+    def set_profiling(self, on=True):
+        self._lib.qses_set_profiling(self._h, int(on))
+
+    def stage_times(self):
+        ms = (ctypes.c_float * 32)()
+        names = (ctypes.c_char_p * 32)()
+        k = self._lib.qses_stage_times(self._h, ms, names, 32)
+        return [(names[q].decode(), float(ms[q])) for q in range(k)]
+
+    def last_launch_count(self):
+        return int(self._lib.qses_last_launch_count(self._h))
+
+
+def grid_info(xyz, radii, voxel):
+    xyz, radii = _f32(xyz, 3), _f32(radii)
+    gi = L.GridInfo()
+    rc = L.lib().qses_grid_info_for(xyz.ctypes.data_as(ctypes.c_void_p),
+                                    radii.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), xyz.shape[0],
+                                    ctypes.c_float(voxel), ctypes.byref(gi))
+    if rc != L.QSES_OK:
+        raise QSESError(rc, "qses_grid_info_for: " + L.status_string(rc))
+    return gi
+
+
+_default_ctx = None
+
+
+def compute_ses(xyz, radii, voxel=0.5, smooth=1, keep_degenerate=False) -> Mesh:
+    """computeSlicedSES + API_computeSES in one call (CudaSurf.cu:524-841)."""
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context()
+    return _default_ctx.compute(xyz, radii, voxel=voxel, smooth=smooth, keep_degenerate=keep_degenerate)
+
+
+class ReferenceAPI:
+    """The API_* symbols exactly as QuickSES exports them (CudaSurf.h:75-83)."""
+
+    def __init__(self):
+        self._lib = L.lib()
+
+    def computeSES(self, reso, xyz, radii, smooth=1):
+        xyz, radii = _f32(xyz, 3), _f32(radii)
+        nv, ntri = ctypes.c_uint(0), ctypes.c_uint(0)
+        self._lib.API_computeSES(ctypes.c_float(reso), xyz.ctypes.data_as(ctypes.c_void_p),
+                                 radii.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), xyz.shape[0], None,
+                                 ctypes.byref(nv), None, ctypes.byref(ntri), int(smooth))
+        rc = self._lib.qses_api_last_status()
+        if rc != L.QSES_OK:
+            raise QSESError(rc, "API_computeSES: " + L.status_string(rc))
+        return nv.value, ntri.value
+
+    def getVertices(self, nv):
+        p = self._lib.API_getVertices()
+        return np.ctypeslib.as_array(p, shape=(nv * 3,)).reshape(nv, 3).copy() if nv else np.zeros((0, 3), np.float32)
+
+    def getTriangles(self, nidx, invert=False):
+        p = self._lib.API_getTriangles(bool(invert))
+        return np.ctypeslib.as_array(p, shape=(nidx,)).copy() if nidx else np.zeros(0, np.int32)
+
+    def getAtomIdPerVert(self, nv):
+        p = self._lib.API_getAtomIdPerVert()
+        return np.ctypeslib.as_array(p, shape=(nv,)).copy() if nv else np.zeros(0, np.int32)
+
+    def freeMesh(self):
+        self._lib.API_freeMesh()
+
+    def exported_counts(self):
+        return (ctypes.c_int.in_dll(self._lib, "NVertices").value, ctypes.c_int.in_dll(self._lib, "NTriangles").value)

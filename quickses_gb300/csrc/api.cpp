@@ -1,0 +1,355 @@
+// C-ABI: QuickSES-compatible API_* surface (CudaSurf.h:75-83, CudaSurf.cu:778-873) and the
+// reentrant qses_* interface.  No entry point exits the process; errors are status codes.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <algorithm>
+#include <new>
+
+#include "kernels.h"
+#include "qses_context.h"
+
+using qses::DeviceMesh;
+
+namespace {
+
+// Host result buffers are pinned so the device-to-host copies run at full link speed.
+struct HostMesh {
+    void *block = nullptr;
+    size_t bytes = 0;
+};
+
+int fill_host_mesh(qses_context *ctx, qses_mesh *out) {
+    const DeviceMesh &m = ctx->mesh;
+    memset(out, 0, sizeof(*out));
+    const size_t vb = 12ull * m.nv, tb = 12ull * m.nt, ab = 4ull * m.nv;
+    const size_t total = vb + tb + 2 * ab + 64;
+    HostMesh *hm = new (std::nothrow) HostMesh();
+    if (!hm) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "host mesh");
+    if (cudaMallocHost(&hm->block, total) != cudaSuccess) {
+        cudaGetLastError();
+        delete hm;
+        return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned host mesh");
+    }
+    hm->bytes = total;
+    char *p = (char *)hm->block;
+    out->vertices = (qses_float3 *)p;
+    out->triangles = (int *)(p + vb);
+    out->atom_sorted = (int *)(p + vb + tb);
+    out->atom_input = (int *)(p + vb + tb + ab);
+    out->n_vertices = m.nv;
+    out->n_triangles = m.nt;
+    out->_owner = hm;
+    if (ctx->have_grid) {
+        out->grid_dim = ctx->grid.G;
+        out->origin[0] = ctx->grid.ox; out->origin[1] = ctx->grid.oy; out->origin[2] = ctx->grid.oz;
+    }
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    if (vb) e = cudaMemcpyAsync(out->vertices, m.vertices, vb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && tb) e = cudaMemcpyAsync(out->triangles, m.triangles, tb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && ab) e = cudaMemcpyAsync(out->atom_sorted, m.atom_sorted, ab, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && ab) e = cudaMemcpyAsync(out->atom_input, m.atom_input, ab, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        qses_mesh_release(out);
+        return ctx->fail(QSES_ERR_CUDA, "mesh download", e);
+    }
+    return QSES_OK;
+}
+
+int empty_mesh(qses_context *ctx, qses_mesh *out) {
+    ctx->mesh = DeviceMesh();
+    ctx->mesh.valid = true;
+    ctx->have_grid = false;
+    return fill_host_mesh(ctx, out);
+}
+
+int check_params(qses_context *ctx, const qses_params *p) {
+    if (!p) return ctx->fail(QSES_ERR_INVALID_ARG, "null parameters");
+    if (!(p->voxel > 0.0f)) return ctx->fail(QSES_ERR_INVALID_ARG, "voxel size must be > 0");
+    if (p->smooth_passes < 0 || p->smooth_passes > 1000)
+        return ctx->fail(QSES_ERR_INVALID_ARG, "smooth_passes must be in [0, 1000]");
+    return QSES_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+QSES_API const char *qses_status_string(int status) {
+    switch (status) {
+        case QSES_OK: return "ok";
+        case QSES_ERR_INVALID_ARG: return "invalid argument";
+        case QSES_ERR_NO_DEVICE: return "no usable sm_103 CUDA device";
+        case QSES_ERR_CUDA: return "CUDA runtime error";
+        case QSES_ERR_OUT_OF_MEMORY: return "out of memory";
+        case QSES_ERR_UNSUPPORTED: return "input outside the supported envelope";
+        case QSES_ERR_TIMEOUT: return "bounded device wait timed out";
+        case QSES_ERR_INTERNAL: return "internal error";
+        default: return "unknown status";
+    }
+}
+
+QSES_API void qses_params_default(qses_params *p) {
+    if (!p) return;
+    p->voxel = 0.5f;
+    p->smooth_passes = 1;
+    p->slice = 300;
+    p->flags = 0;
+}
+
+QSES_API int qses_context_create(int device, void *cuda_stream, qses_context **out) {
+    if (!out) return QSES_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        return QSES_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || prop.major != 10 || prop.minor != 3) {
+        cudaGetLastError();
+        return QSES_ERR_NO_DEVICE;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return QSES_ERR_CUDA;
+    qses_context *ctx = new (std::nothrow) qses_context();
+    if (!ctx) return QSES_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    if (cuda_stream) {
+        ctx->stream = (cudaStream_t)cuda_stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete ctx;
+            return QSES_ERR_CUDA;
+        }
+        ctx->own_stream = true;
+    }
+    if (cudaMalloc(&ctx->small, 4096) != cudaSuccess || cudaMallocHost((void **)&ctx->h_small, 4096) != cudaSuccess) {
+        cudaGetLastError();
+        qses_context_destroy(ctx);
+        return QSES_ERR_OUT_OF_MEMORY;
+    }
+    int maxb = qses::gs_max_blocks(device);
+    ctx->gs_blocks = maxb < 16 ? maxb : 16;
+    *out = ctx;
+    return QSES_OK;
+}
+
+QSES_API int qses_context_destroy(qses_context *ctx) {
+    if (!ctx) return QSES_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->input.release();
+    ctx->field.release();
+    ctx->mesh_ws.release();
+    if (ctx->small) cudaFree(ctx->small);
+    if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    for (auto &m : ctx->marks) cudaEventDestroy(m.second);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return QSES_OK;
+}
+
+QSES_API int qses_compute(qses_context *ctx, const qses_params *p, const qses_float3 *atoms, const float *radii,
+                          unsigned n, qses_mesh *out) {
+    if (!ctx || !out) return QSES_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    int rc = check_params(ctx, p);
+    if (rc) return rc;
+    if (n > 0 && (!atoms || !radii)) return ctx->fail(QSES_ERR_INVALID_ARG, "null atom arrays");
+    cudaSetDevice(ctx->device);
+    if (n <= 1) return empty_mesh(ctx, out);  // CudaSurf.cu:539-543
+    if (ctx->input.reserve(16ull * n + 512) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "input buffers");
+    float *d_xyz = (float *)ctx->input.take(12ull * n);
+    float *d_r = (float *)ctx->input.take(4ull * n);
+    cudaError_t e = cudaMemcpyAsync(d_xyz, atoms, 12ull * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_r, radii, 4ull * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return ctx->fail(QSES_ERR_CUDA, "atom upload", e);
+    rc = qses::run_pipeline(ctx, *p, d_xyz, d_r, n);
+    if (rc) return rc;
+    return fill_host_mesh(ctx, out);
+}
+
+QSES_API int qses_compute_device(qses_context *ctx, const qses_params *p, const float *d_xyz, const float *d_radii,
+                                 unsigned n, qses_device_mesh *out) {
+    if (!ctx || !out) return QSES_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    int rc = check_params(ctx, p);
+    if (rc) return rc;
+    cudaSetDevice(ctx->device);
+    if (n <= 1) {
+        ctx->mesh = DeviceMesh();
+        ctx->mesh.valid = true;
+        return QSES_OK;
+    }
+    if (!d_xyz || !d_radii) return ctx->fail(QSES_ERR_INVALID_ARG, "null atom arrays");
+    rc = qses::run_pipeline(ctx, *p, d_xyz, d_radii, n);
+    if (rc) return rc;
+    out->n_vertices = ctx->mesh.nv;
+    out->n_triangles = ctx->mesh.nt;
+    out->d_vertices = ctx->mesh.vertices;
+    out->d_triangles = (int *)ctx->mesh.triangles;
+    out->d_atom_sorted = ctx->mesh.atom_sorted;
+    out->d_atom_input = ctx->mesh.atom_input;
+    return QSES_OK;
+}
+
+QSES_API void qses_mesh_release(qses_mesh *m) {
+    if (!m) return;
+    HostMesh *hm = (HostMesh *)m->_owner;
+    if (hm) {
+        if (hm->block) cudaFreeHost(hm->block);
+        delete hm;
+    }
+    memset(m, 0, sizeof(*m));
+}
+
+QSES_API const char *qses_last_error(qses_context *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+QSES_API int qses_set_profiling(qses_context *ctx, int on) {
+    if (!ctx) return QSES_ERR_INVALID_ARG;
+    ctx->profiling = on != 0;
+    return QSES_OK;
+}
+
+QSES_API int qses_stage_times(qses_context *ctx, float *ms, const char **names, int max) {
+    if (!ctx) return 0;
+    int k = 0;
+    for (auto &t : ctx->times) {
+        if (k >= max) break;
+        if (ms) ms[k] = t.second;
+        if (names) names[k] = t.first;
+        k++;
+    }
+    return k;
+}
+
+QSES_API int qses_last_launch_count(qses_context *ctx) { return ctx ? ctx->launches : 0; }
+
+QSES_API int qses_grid_info_for(const qses_float3 *atoms, const float *radii, unsigned n, float voxel,
+                                qses_grid_info *out) {
+    if (!atoms || !radii || !out || n == 0) return QSES_ERR_INVALID_ARG;
+    float mn[3] = {100000.0f, 100000.0f, 100000.0f}, mx[3] = {-100000.0f, -100000.0f, -100000.0f}, maxR = 0.0f;
+    for (unsigned a = 0; a < n; a++) {
+        const float c[3] = {atoms[a].x, atoms[a].y, atoms[a].z};
+        for (int q = 0; q < 3; q++) {
+            mn[q] = std::min(mn[q], c[q]);
+            mx[q] = std::max(mx[q], c[q]);
+        }
+        maxR = std::max(maxR, radii[a]);
+    }
+    QGrid g;
+    return qses::grid_from_bounds(mn, mx, maxR, n, voxel, g, out, nullptr);
+}
+
+QSES_API int qses_debug_codes(qses_context *ctx, uint8_t *codes, size_t bytes) {
+    if (!ctx || !codes || !ctx->mesh.valid || !ctx->have_grid || !ctx->mesh.codes) return QSES_ERR_INVALID_ARG;
+    const size_t G = (size_t)ctx->grid.G;
+    if (bytes < G * G * G) return QSES_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMemcpy2DAsync(codes, G, ctx->mesh.codes, (size_t)ctx->grid.Gp, G, G * G,
+                                      cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? QSES_OK : ctx->fail(QSES_ERR_CUDA, "codes download", e);
+}
+
+QSES_API int qses_debug_atom_order(qses_context *ctx, uint32_t *sorted_to_input, uint32_t *hash, unsigned n) {
+    if (!ctx || !ctx->mesh.valid || !ctx->mesh.sorted_to_input || n != ctx->mesh.n_atoms) return QSES_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaSuccess;
+    if (sorted_to_input)
+        e = cudaMemcpyAsync(sorted_to_input, ctx->mesh.sorted_to_input, 4ull * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && hash)
+        e = cudaMemcpyAsync(hash, ctx->mesh.sorted_keys, 4ull * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? QSES_OK : ctx->fail(QSES_ERR_CUDA, "atom order download", e);
+}
+
+// ------------------------------------------------------------ QuickSES surface
+
+QSES_API int NTriangles = 0;
+QSES_API int NVertices = 0;
+QSES_API int *globalTriangles = nullptr;
+QSES_API qses_float3 *globalVertices = nullptr;
+QSES_API int *globalIdAtomPerVert = nullptr;
+
+}  // extern "C"
+
+namespace {
+std::mutex g_api_mu;
+qses_context *g_api_ctx = nullptr;
+qses_mesh g_api_mesh;
+int g_api_status = QSES_OK;
+}  // namespace
+
+extern "C" {
+
+QSES_API int qses_api_last_status(void) { return g_api_status; }
+
+QSES_API void API_computeSES(float resoSES, qses_float3 *atomPos, float *atomRad, unsigned int N,
+                             qses_float3 *out_vertices, unsigned int *NVert, int *out_triangles, unsigned int *NTri,
+                             int doSmoothing) {
+    (void)out_vertices;
+    (void)out_triangles;  // ignored, as in the reference (CudaSurf.cu:839-840)
+    std::lock_guard<std::mutex> lock(g_api_mu);
+    if (NVert) *NVert = 0;
+    if (NTri) *NTri = 0;
+    if (!g_api_ctx) {
+        g_api_status = qses_context_create(0, nullptr, &g_api_ctx);
+        if (g_api_status != QSES_OK) {
+            fprintf(stderr, "quickses_gb300: %s\n", qses_status_string(g_api_status));
+            return;
+        }
+    }
+    qses_params p;
+    qses_params_default(&p);
+    p.voxel = resoSES;
+    p.smooth_passes = doSmoothing < 0 ? 0 : doSmoothing;
+    qses_mesh m;
+    g_api_status = qses_compute(g_api_ctx, &p, atomPos, atomRad, N, &m);
+    if (g_api_status != QSES_OK) {
+        fprintf(stderr, "quickses_gb300: %s\n", qses_last_error(g_api_ctx));
+        return;
+    }
+    // Like the reference, a second call without API_freeMesh does not free the previous
+    // buffers; the globals simply point at the new ones.
+    g_api_mesh = m;
+    globalVertices = m.vertices;
+    globalTriangles = m.triangles;
+    globalIdAtomPerVert = m.atom_sorted;
+    NVertices = (int)m.n_vertices;
+    NTriangles = (int)(3 * m.n_triangles);
+    if (NVert) *NVert = m.n_vertices;
+    if (NTri) *NTri = 3 * m.n_triangles;
+}
+
+QSES_API int *API_getTriangles(bool invertTriangles) {
+    if (invertTriangles && globalTriangles) {
+        for (int t = 0; t < NTriangles / 3; t++) {
+            int save = globalTriangles[3 * t];
+            globalTriangles[3 * t] = globalTriangles[3 * t + 1];
+            globalTriangles[3 * t + 1] = save;
+        }
+    }
+    return globalTriangles;
+}
+
+QSES_API qses_float3 *API_getVertices(void) { return globalVertices; }
+
+QSES_API int *API_getAtomIdPerVert(void) { return globalIdAtomPerVert; }
+
+QSES_API void API_freeMesh(void) {
+    std::lock_guard<std::mutex> lock(g_api_mu);
+    qses_mesh_release(&g_api_mesh);
+    globalVertices = nullptr;
+    globalTriangles = nullptr;
+    globalIdAtomPerVert = nullptr;
+    NVertices = 0;
+    NTriangles = 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,364 @@
+// Atom grid and SES distance field.
+//
+//  k_atom_minmax  bbox + largest radius for the grid sizing (getMinMax, CudaSurf.cu:149-174)
+//  k_atom_hash    neighbour-cell key per atom (hashAtoms, Kernels.cu:185-216)
+//  k_atom_gather  cell-sorted xyzr + cell start/end (sortCell, Kernels.cu:306-341)
+//  k_sas          SAS classification, 8x8 rows x 32 voxels per CTA, atoms staged in shared
+//                 memory, row intervals found analytically and verified with the exact
+//                 per-voxel predicate (computeInOrOut / probeIntersection, Kernels.cu:344-475)
+//  k_edt          probe refine as an exact windowed squared distance transform over the
+//                 outside bitmask (distanceFieldRefine, Kernels.cu:478-545)
+//
+// Field values are stored as one byte per voxel: n in [0, 3R^2] is the squared voxel
+// distance to the nearest outside voxel (value probe - dx*sqrt(n)), 253 = border voxel
+// with no outside voxel in its window (-dx), 254 = inside (-dx), 255 = outside (probe).
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace qses {
+
+// ---------------------------------------------------------------- atoms
+
+__device__ __forceinline__ unsigned enc_f(float f) {
+    unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__global__ void k_atom_minmax(const float *__restrict__ xyz, const float *__restrict__ r, unsigned n,
+                              unsigned *mm /* 7: min xyz, max xyz, max r (order-preserving encodings) */) {
+    unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[4] = {0u, 0u, 0u, 0u};
+    for (size_t a = (size_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            unsigned e = enc_f(xyz[3 * a + c]);
+            lo[c] = min(lo[c], e);
+            hi[c] = max(hi[c], e);
+        }
+        hi[3] = max(hi[3], enc_f(r[a]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            lo[c] = min(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+            hi[c] = max(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+        }
+        hi[3] = max(hi[3], __shfl_xor_sync(0xffffffffu, hi[3], o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int c = 0; c < 3; c++) {
+            atomicMin(&mm[c], lo[c]);
+            atomicMax(&mm[3 + c], hi[c]);
+        }
+        atomicMax(&mm[6], hi[3]);
+    }
+}
+
+__global__ void k_atom_hash(QGrid g, const float *__restrict__ xyz, unsigned n, unsigned *__restrict__ key) {
+    unsigned a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    // spaceToGrid: truncating IEEE division, then flatten3DTo1D (Kernels.cu:119-131).
+    int cx = __float2int_rz(__fdiv_rn(__fsub_rn(xyz[3 * a], g.ox), g.cell));
+    int cy = __float2int_rz(__fdiv_rn(__fsub_rn(xyz[3 * a + 1], g.oy), g.cell));
+    int cz = __float2int_rz(__fdiv_rn(__fsub_rn(xyz[3 * a + 2], g.oz), g.cell));
+    key[a] = (unsigned)(g.gnb * g.gnb * cx + g.gnb * cy + cz);
+}
+
+__global__ void k_atom_gather(const float *__restrict__ xyz, const float *__restrict__ r,
+                              const unsigned *__restrict__ skey, const unsigned *__restrict__ sidx, unsigned n,
+                              float4 *__restrict__ atoms, uint2 *__restrict__ cells) {
+    unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    unsigned a = sidx[s];
+    atoms[s] = make_float4(xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2], r[a]);
+    unsigned k = skey[s];
+    if (s == 0 || skey[s - 1] != k) cells[k].x = s;
+    if (s == n - 1 || skey[s + 1] != k) cells[k].y = s + 1;
+}
+
+// ------------------------------------------------------------------ SAS
+
+constexpr int kSasTX = 8, kSasTY = 8, kSasNT = kSasTX * kSasTY, kSasCap = 768;
+
+// Exact per-voxel test along a z row: fma(ez, ez, sxy) < t with ez = z(k) - az.
+__device__ __forceinline__ bool zpred(int k, float az, float sxy, float t, float dx, float oz) {
+    float ez = __fsub_rn(vox(k, dx, oz), az);
+    return __fmaf_rn(ez, ez, sxy) < t;
+}
+
+__device__ __forceinline__ unsigned span_bits(int a, int b) {  // bits a..b inclusive, 0 <= a <= b <= 31
+    unsigned m = (b - a == 31) ? 0xffffffffu : ((1u << (b - a + 1)) - 1u);
+    return m << a;
+}
+
+// Voxels k in [k0, klim] of one z row whose squared distance to the atom is below t.
+// The set is an interval (the predicate is monotone in |k - k_atom|); its ends are
+// estimated in closed form and verified with the exact predicate, with a brute-force
+// fallback if the estimate does not verify.
+__device__ unsigned zmask(float az, float sxy, float t, int k0, int klim, float dx, float oz, float inv_dx) {
+    float kcf = fminf(fmaxf((az - oz) * inv_dx, -1.0e6f), 1.0e6f);
+    float h = sqrtf(fmaxf(t - sxy, 0.0f)) * inv_dx;
+    int lo = max(k0, (int)ceilf(kcf - h));
+    int hi = min(klim, (int)floorf(kcf + h));
+    if (lo <= hi) {
+        if (zpred(lo, az, sxy, t, dx, oz) && zpred(hi, az, sxy, t, dx, oz) &&
+            (lo == k0 || !zpred(lo - 1, az, sxy, t, dx, oz)) && (hi == klim || !zpred(hi + 1, az, sxy, t, dx, oz)))
+            return span_bits(lo - k0, hi - k0);
+    } else {
+        int c = min(max(__float2int_rn(kcf), k0), klim);
+        if (!zpred(c, az, sxy, t, dx, oz) && (c == k0 || !zpred(c - 1, az, sxy, t, dx, oz)) &&
+            (c == klim || !zpred(c + 1, az, sxy, t, dx, oz)))
+            return 0u;
+    }
+    unsigned m = 0;
+    for (int k = k0; k <= klim; k++)
+        if (zpred(k, az, sxy, t, dx, oz)) m |= 1u << (k - k0);
+    return m;
+}
+
+// Row-interval classification of one z row against one atom.
+__device__ __forceinline__ void sas_row_atom(float px, float py, float ax, float ay, float az, float tin, float tsas,
+                                             int k0, int klim, const QGrid &g, float inv_dx, unsigned &sasw,
+                                             unsigned &inw) {
+    float ex = __fsub_rn(px, ax), ey = __fsub_rn(py, ay);
+    float sxy = __fmaf_rn(ey, ey, __fmul_rn(ex, ex));
+    if (sxy < tsas) {
+        sasw |= zmask(az, sxy, tsas, k0, klim, g.dx, g.oz, inv_dx);
+        if (sxy < tin) inw |= zmask(az, sxy, tin, k0, klim, g.dx, g.oz, inv_dx);
+    }
+}
+
+__device__ __forceinline__ void atom_thresholds(float r, const QGrid &g, float &tin, float &tsas) {
+    float rin = __fsub_rn(r, g.dx);                        // d < r - dx  (Kernels.cu:377)
+    tin = rin > 0.0f ? __fmul_rn(rin, rin) : -1.0f;
+    float rs = __fadd_rn(g.probe, r);                      // d < probe + r  (Kernels.cu:380)
+    tsas = __fmul_rn(rs, rs);
+}
+
+__global__ void __launch_bounds__(kSasNT) k_sas(QGrid g, const float4 *__restrict__ atoms,
+                                                const uint2 *__restrict__ cells, unsigned *__restrict__ inMask,
+                                                unsigned *__restrict__ outMask) {
+    __shared__ float s_x[kSasCap], s_y[kSasCap], s_z[kSasCap], s_tin[kSasCap], s_ts[kSasCap];
+    __shared__ int s_n, s_over;
+    const int w = blockIdx.x, j0 = blockIdx.y * kSasTY, i0 = blockIdx.z * kSasTX;
+    const int t = threadIdx.x, i = i0 + t / kSasTY, j = j0 + t % kSasTY, k0 = w * 32;
+    const int G = g.G, last = G - 2;  // voxels with an index of G-1 are never computed (Kernels.cu:436-441)
+    const unsigned valid = (k0 + 32 <= G) ? 0xffffffffu : ((1u << (G - k0)) - 1u);
+    const unsigned lastbit = (G - 1 >= k0 && G - 1 < k0 + 32) ? (1u << (G - 1 - k0)) : 0u;
+    const int klim = min(k0 + 31, last);
+    const float inv_dx = 1.0f / g.dx;
+    unsigned sasw = 0, inw = 0;
+
+    if (i0 <= last && j0 <= last && k0 <= last) {
+        const float bx0 = vox(i0, g.dx, g.ox), bx1 = vox(min(i0 + kSasTX - 1, last), g.dx, g.ox);
+        const float by0 = vox(j0, g.dx, g.oy), by1 = vox(min(j0 + kSasTY - 1, last), g.dx, g.oy);
+        const float bz0 = vox(k0, g.dx, g.oz), bz1 = vox(klim, g.dx, g.oz);
+        const float ext = g.cell * 1.01f + g.dx;
+        auto crange = [&](float lo, float hi, float o, int &c0, int &c1) {
+            c0 = min(max((int)floorf((lo - ext - o) / g.cell), 0), g.gnb - 1);
+            c1 = min(max((int)floorf((hi + ext - o) / g.cell), 0), g.gnb - 1);
+        };
+        int cx0, cx1, cy0, cy1, cz0, cz1;
+        crange(bx0, bx1, g.ox, cx0, cx1);
+        crange(by0, by1, g.oy, cy0, cy1);
+        crange(bz0, bz1, g.oz, cz0, cz1);
+        const int ncy = cy1 - cy0 + 1, ncz = cz1 - cz0 + 1, ncell = (cx1 - cx0 + 1) * ncy * ncz;
+        if (t == 0) { s_n = 0; s_over = 0; }
+        __syncthreads();
+        // Stage every atom whose probe-inflated sphere can reach the tile (conservative box test).
+        for (int c = t; c < ncell; c += kSasNT) {
+            int cz = c % ncz, cy = (c / ncz) % ncy, cx = c / (ncz * ncy);
+            uint2 rg = cells[((size_t)(cx0 + cx) * g.gnb + (cy0 + cy)) * g.gnb + (cz0 + cz)];
+            for (unsigned s = rg.x; s < rg.y; s++) {
+                float4 a = atoms[s];
+                float ddx = fmaxf(fmaxf(bx0 - a.x, a.x - bx1), 0.0f);
+                float ddy = fmaxf(fmaxf(by0 - a.y, a.y - by1), 0.0f);
+                float ddz = fmaxf(fmaxf(bz0 - a.z, a.z - bz1), 0.0f);
+                float rs = g.probe + a.w;
+                if (ddx * ddx + ddy * ddy + ddz * ddz <= rs * rs * 1.001f + 1e-3f) {
+                    int q = atomicAdd(&s_n, 1);
+                    if (q < kSasCap) {
+                        float tin, tsas;
+                        atom_thresholds(a.w, g, tin, tsas);
+                        s_x[q] = a.x; s_y[q] = a.y; s_z[q] = a.z; s_tin[q] = tin; s_ts[q] = tsas;
+                    } else {
+                        s_over = 1;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (i <= last && j <= last) {
+            const float px = vox(i, g.dx, g.ox), py = vox(j, g.dx, g.oy);
+            if (!s_over) {
+                const int na = s_n;
+                for (int q = 0; q < na; q++)
+                    sas_row_atom(px, py, s_x[q], s_y[q], s_z[q], s_tin[q], s_ts[q], k0, klim, g, inv_dx, sasw, inw);
+            } else {
+                // Too many candidates for shared memory: walk the cells directly.
+                for (int c = 0; c < ncell; c++) {
+                    int cz = c % ncz, cy = (c / ncz) % ncy, cx = c / (ncz * ncy);
+                    uint2 rg = cells[((size_t)(cx0 + cx) * g.gnb + (cy0 + cy)) * g.gnb + (cz0 + cz)];
+                    for (unsigned s = rg.x; s < rg.y; s++) {
+                        float4 a = atoms[s];
+                        float tin, tsas;
+                        atom_thresholds(a.w, g, tin, tsas);
+                        sas_row_atom(px, py, a.x, a.y, a.z, tin, tsas, k0, klim, g, inv_dx, sasw, inw);
+                    }
+                }
+            }
+        }
+    }
+    if (i < G && j < G) {
+        unsigned outw, inw2;
+        if (i >= G - 1 || j >= G - 1) {
+            outw = valid;
+            inw2 = 0u;
+        } else {
+            outw = (~sasw & valid) | lastbit;
+            inw2 = inw & ~lastbit;
+        }
+        size_t idx = ((size_t)i * G + j) * g.W + w;
+        inMask[idx] = inw2;
+        outMask[idx] = outw;
+    }
+}
+
+// ------------------------------------------------------------------ refine
+
+constexpr int kEdtTX = 8, kEdtTY = 8, kEdtNT = 256, kEdtH = kEdtTX + 2 * QSES_RMAX;
+
+__global__ void __launch_bounds__(kEdtNT) k_edt(QGrid g, const unsigned *__restrict__ inMask,
+                                                const unsigned *__restrict__ outMask,
+                                                unsigned char *__restrict__ codes, unsigned *__restrict__ signMask) {
+    __shared__ unsigned s_out[kEdtH * kEdtH][3];
+    __shared__ unsigned char s_g[kEdtH * kEdtH][32];
+    __shared__ unsigned char s_h[kEdtH][kEdtTY][32];
+    __shared__ unsigned s_in[kEdtTX * kEdtTY], s_ot[kEdtTX * kEdtTY];
+    const int w = blockIdx.x, j0 = blockIdx.y * kEdtTY, i0 = blockIdx.z * kEdtTX;
+    const int R = g.R, G = g.G, W = g.W, t = threadIdx.x;
+    const int HX = kEdtTX + 2 * R, HY = kEdtTY + 2 * R, k0 = w * 32;
+    const unsigned valid = (k0 + 32 <= G) ? 0xffffffffu : ((1u << (G - k0)) - 1u);
+
+    int anyb = 0;
+    if (t < kEdtTX * kEdtTY) {
+        int i = i0 + t / kEdtTY, j = j0 + t % kEdtTY;
+        unsigned iw = 0u, ow = 0xffffffffu;
+        if (i < G && j < G) {
+            size_t idx = ((size_t)i * G + j) * W + w;
+            iw = inMask[idx];
+            ow = outMask[idx];
+            anyb = (valid & ~iw & ~ow) != 0u;
+        }
+        s_in[t] = iw;
+        s_ot[t] = ow;
+    }
+    const int has_border = __syncthreads_or(anyb);
+    int has_out = 0;
+    if (has_border) {
+        int any = 0;
+        for (int q = t; q < HX * HY; q += kEdtNT) {
+            int i = i0 - R + q / HY, j = j0 - R + q % HY;
+            unsigned a = 0u, b = 0u, c = 0u;
+            if (i >= 0 && i < G && j >= 0 && j < G) {
+                size_t base = ((size_t)i * G + j) * W;
+                if (w > 0) a = outMask[base + w - 1];
+                b = outMask[base + w];
+                if (w + 1 < W) c = outMask[base + w + 1];
+            }
+            s_out[q][0] = a; s_out[q][1] = b; s_out[q][2] = c;
+            any |= (a | b | c) != 0u;
+        }
+        has_out = __syncthreads_or(any);
+    }
+    if (has_border && has_out) {
+        // z: distance (in voxels, <= R) to the nearest outside voxel along the row.
+        for (int q = t; q < HX * HY * 32; q += kEdtNT) {
+            const int row = q >> 5, b = q & 31;
+            const unsigned a = s_out[row][0], c = s_out[row][1], d = s_out[row][2];
+            unsigned char gv = 255;
+            if (a | c | d) {
+                unsigned long long up = (((unsigned long long)d << 32) | c) >> b;
+                int du = up ? (__ffsll((long long)up) - 1) : 1000;
+                unsigned long long dn = (((unsigned long long)c << 32) | a) << (31 - b);
+                int dd = dn ? __clzll((long long)dn) : 1000;
+                int m = min(du, dd);
+                if (m <= R) gv = (unsigned char)m;
+            }
+            s_g[row][b] = gv;
+        }
+        __syncthreads();
+        // y: min over dj of dj^2 + g^2.
+        for (int q = t; q < HX * kEdtTY * 32; q += kEdtNT) {
+            const int b = q & 31, y = (q >> 5) % kEdtTY, hx = (q >> 5) / kEdtTY;
+            int best = 255;
+            for (int dj = -R; dj <= R; dj++) {
+                int gv = s_g[hx * HY + y + R + dj][b];
+                if (gv != 255) best = min(best, dj * dj + gv * gv);
+            }
+            s_h[hx][y][b] = (unsigned char)best;
+        }
+        __syncthreads();
+    }
+    // x: min over di of di^2 + h, then codes and sign bits; 4 threads per row, 8 voxels each.
+    const int row = t >> 2, part = t & 3, x = row / kEdtTY, y = row % kEdtTY, i = i0 + x, j = j0 + y;
+    unsigned sgn = 0u;
+    if (i < G && j < G) {
+        const unsigned iw = s_in[row], ow = s_ot[row];
+        unsigned long long packed = 0ull;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int b = part * 8 + e;
+            const unsigned bit = 1u << b;
+            unsigned code;
+            if (!(valid & bit)) code = QSES_CODE_OUT;  // row padding, never read
+            else if (ow & bit) code = QSES_CODE_OUT;
+            else if (iw & bit) code = QSES_CODE_IN;
+            else {
+                code = QSES_CODE_NONE;
+                if (has_out) {
+                    int best = 255;
+                    for (int di = -R; di <= R; di++) {
+                        int hv = s_h[x + R + di][y][b];
+                        if (hv != 255) best = min(best, di * di + hv);
+                    }
+                    if (best != 255) code = (unsigned)best;
+                }
+            }
+            packed |= (unsigned long long)code << (8 * e);
+            if ((valid & bit) && code != QSES_CODE_OUT && (int)code >= g.negmin) sgn |= bit;
+        }
+        *(unsigned long long *)(codes + ((size_t)i * G + j) * g.Gp + k0 + part * 8) = packed;
+    }
+    sgn |= __shfl_xor_sync(0xffffffffu, sgn, 1);
+    sgn |= __shfl_xor_sync(0xffffffffu, sgn, 2);
+    if (part == 0 && i < G && j < G) signMask[((size_t)i * G + j) * W + w] = sgn;
+}
+
+// ------------------------------------------------------------ launchers
+
+void launch_atom_minmax(const float *xyz, const float *r, unsigned n, unsigned *mm, cudaStream_t s) {
+    unsigned blocks = (n + 255) / 256;
+    if (blocks > 608) blocks = 608;
+    if (blocks == 0) blocks = 1;
+    k_atom_minmax<<<blocks, 256, 0, s>>>(xyz, r, n, mm);
+}
+void launch_atom_hash(const QGrid &g, const float *xyz, unsigned n, unsigned *key, cudaStream_t s) {
+    k_atom_hash<<<(n + 255) / 256, 256, 0, s>>>(g, xyz, n, key);
+}
+void launch_atom_gather(const float *xyz, const float *r, const unsigned *skey, const unsigned *sidx, unsigned n,
+                        float4 *atoms, uint2 *cells, cudaStream_t s) {
+    k_atom_gather<<<(n + 255) / 256, 256, 0, s>>>(xyz, r, skey, sidx, n, atoms, cells);
+}
+void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigned *inMask, unsigned *outMask,
+                cudaStream_t s) {
+    dim3 grid(g.W, (g.G + kSasTY - 1) / kSasTY, (g.G + kSasTX - 1) / kSasTX);
+    k_sas<<<grid, kSasNT, 0, s>>>(g, atoms, cells, inMask, outMask);
+}
+void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
+                unsigned *signMask, cudaStream_t s) {
+    dim3 grid(g.W, (g.G + kEdtTY - 1) / kEdtTY, (g.G + kEdtTX - 1) / kEdtTX);
+    k_edt<<<grid, kEdtNT, 0, s>>>(g, inMask, outMask, codes, signMask);
+}
+
+}  // namespace qses

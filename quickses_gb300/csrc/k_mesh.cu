@@ -1,0 +1,450 @@
+// Marching cubes, vertex weld, closest atom, degenerate filter and Laplacian smoothing.
+//
+//  k_mc<false>    per (x, y) row of cells: triangle count and active-edge count
+//                 (countVertexPerCell, MarchingCubes.cu:571-658, single-slice cell range)
+//  k_mc<true>     the same rows again: triangles in cell linear order x*G^2 + y*G + z and
+//                 one quantised key per active edge (generateTriangleVerticesSMEM +
+//                 groupVertices, MarchingCubes.cu:736-862).  One warp per row; the sign of
+//                 32 voxels is one word, so cube indices and edge activity are bit ops.
+//  k_weld_*       unique quantised positions in lexicographic order (CudaSurf.cu:444-457)
+//  k_closest      closest atom per welded vertex (closestAtomPerVertex, Kernels.cu:547-604)
+//  k_tri_*        drop triangles with a repeated index (CudaSurf.cu:820-829)
+//  k_csr_* / k_gs neighbour lists in triangle order and the in-place Gauss-Seidel Laplacian
+//                 in vertex-id order (SmoothMesh.cpp:45-123), run as a dataflow: a vertex is
+//                 updated once every lower-id neighbour has been, exactly as the sequential
+//                 loop would see them.
+#include <cfloat>
+
+#include "device_common.cuh"
+#include "kernels.h"
+#include "mc_tables.h"
+
+namespace qses {
+
+__constant__ unsigned long long c_mc[256] = QSES_MC_TABLE_INIT;
+
+// Owner of each cube edge relative to the cell: bit0 di, bit1 dj, bit2 dk, bits3-4 axis.
+// Edges follow MarchingCubes.cu:814-825 with corners as in :625-632.
+constexpr unsigned long long kEdgeOwner =
+    (0ull << 0) | (9ull << 5) | (2ull << 10) | (8ull << 15) | (4ull << 20) | (13ull << 25) | (6ull << 30) |
+    (12ull << 35) | (16ull << 40) | (17ull << 45) | (19ull << 50) | (18ull << 55);
+
+__device__ __forceinline__ unsigned ld_sign(const unsigned *__restrict__ sign, const QGrid &g, int i, int j, int w) {
+    if (i >= g.G || j >= g.G || w >= g.W) return 0u;
+    return __ldg(&sign[((size_t)i * g.G + j) * g.W + w]);
+}
+
+__device__ __forceinline__ unsigned cube_index(unsigned b, unsigned c0, unsigned c1, unsigned c2, unsigned c3,
+                                               unsigned c4, unsigned c5, unsigned c6, unsigned c7) {
+    return ((c0 >> b) & 1u) | (((c1 >> b) & 1u) << 1) | (((c2 >> b) & 1u) << 2) | (((c3 >> b) & 1u) << 3) |
+           (((c4 >> b) & 1u) << 4) | (((c5 >> b) & 1u) << 5) | (((c6 >> b) & 1u) << 6) | (((c7 >> b) & 1u) << 7);
+}
+
+__device__ __forceinline__ unsigned warp_sum(unsigned v) { return __reduce_add_sync(0xffffffffu, v); }
+
+// Quantised key of the vertex on edge (i, j, k) -> (i, j, k) + e_axis.
+__device__ unsigned long long edge_key(const QGrid &g, const unsigned char *__restrict__ codes, const float *lut,
+                                       int i, int j, int k, int ax) {
+    const size_t base = ((size_t)i * g.G + j) * g.Gp + k;
+    const size_t step = ax == 0 ? (size_t)g.G * g.Gp : (ax == 1 ? (size_t)g.Gp : (size_t)1);
+    const float fa = lut[__ldg(codes + base)], fb = lut[__ldg(codes + base + step)];
+    const float t = __fdiv_rn(-fa, __fsub_rn(fb, fa));  // vertexInterp (MarchingCubes.cu:731-734)
+    float p[3] = {vox(i, g.dx, g.ox), vox(j, g.dx, g.oy), vox(k, g.dx, g.oz)};
+    const float o[3] = {g.ox, g.oy, g.oz};
+    const int idx[3] = {i, j, k};
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        if (c == ax) p[c] = __fmaf_rn(t, __fsub_rn(vox(idx[c] + 1, g.dx, o[c]), p[c]), p[c]);
+    // groupVertices: round(v / 0.001) (MarchingCubes.cu:859)
+    long long mx = (long long)roundf(__fdiv_rn(p[0], QSES_WELD_TOL));
+    long long my = (long long)roundf(__fdiv_rn(p[1], QSES_WELD_TOL));
+    long long mz = (long long)roundf(__fdiv_rn(p[2], QSES_WELD_TOL));
+    return ((unsigned long long)(mx - g.bx) * (unsigned long long)g.Rq + (unsigned long long)(my - g.by)) *
+               (unsigned long long)g.Rq +
+           (unsigned long long)(mz - g.bz);
+}
+
+__device__ __forceinline__ unsigned sel4(int o, unsigned a, unsigned b, unsigned c, unsigned d) {
+    return o == 0 ? a : (o == 1 ? b : (o == 2 ? c : d));
+}
+
+template <bool EMIT>
+__global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict__ sign,
+                                            const unsigned char *__restrict__ codes, const float *__restrict__ lut,
+                                            uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
+                                            unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey) {
+    __shared__ unsigned long long s_tab[256];
+    __shared__ float s_lut[256];
+    s_tab[threadIdx.x] = c_mc[threadIdx.x];
+    if (EMIT) s_lut[threadIdx.x] = lut[threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int Gc = g.Gc, E = Gc + 1;
+    const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= (long long)E * E) return;
+    const int i = (int)(row / E), j = (int)(row % E);
+    const bool cellsRow = i < Gc && j < Gc;
+    const int Wc = (Gc + 32) / 32;  // words holding voxels 0..Gc
+
+    unsigned triBase = 0, eb0 = 0, eb1 = 0, eb2 = 0, eb3 = 0;  // owners (0,0) (0,1) (1,0) (1,1)
+    if (EMIT) {
+        triBase = rowBase[row].x;
+        eb0 = rowBase[row].y;
+        if (j + 1 <= Gc) eb1 = rowBase[(size_t)i * E + j + 1].y;
+        if (i + 1 <= Gc) eb2 = rowBase[(size_t)(i + 1) * E + j].y;
+        if (i + 1 <= Gc && j + 1 <= Gc) eb3 = rowBase[(size_t)(i + 1) * E + j + 1].y;
+    }
+    unsigned triCarry = 0, ec0 = 0, ec1 = 0, ec2 = 0, ec3 = 0;
+    for (int w0 = 0; w0 < Wc; w0 += 32) {
+        const int w = w0 + lane;
+        const bool act = w < Wc;
+        const int kb = w * 32;
+        unsigned kv = 0u, kc = 0u;
+        if (act) {
+            int nvx = Gc - kb + 1;  // voxels kb..Gc
+            kv = nvx >= 32 ? 0xffffffffu : ((1u << nvx) - 1u);
+            int ncl = Gc - kb;      // cells / z-edges kb..Gc-1
+            kc = ncl >= 32 ? 0xffffffffu : (ncl <= 0 ? 0u : ((1u << ncl) - 1u));
+        }
+        const bool nxt = act && (kb + 32 <= Gc);
+        auto L = [&](int a, int b, int ww) { return act ? ld_sign(sign, g, i + a, j + b, ww) : 0u; };
+        const unsigned S00 = L(0, 0, w), S10 = L(1, 0, w), S01 = L(0, 1, w), S11 = L(1, 1, w);
+        const unsigned N00 = L(0, 0, w + 1), N10 = L(1, 0, w + 1), N01 = L(0, 1, w + 1), N11 = L(1, 1, w + 1);
+        const unsigned P00 = (S00 >> 1) | (N00 << 31), P10 = (S10 >> 1) | (N10 << 31);
+        const unsigned P01 = (S01 >> 1) | (N01 << 31), P11 = (S11 >> 1) | (N11 << 31);
+        const unsigned X00 = i < Gc ? (S00 ^ S10) & kv : 0u;
+        const unsigned Y00 = j < Gc ? (S00 ^ S01) & kv : 0u;
+        const unsigned Z00 = (S00 ^ P00) & kc;
+        const unsigned c00 = __popc(X00) + __popc(Y00) + __popc(Z00);
+        unsigned cellm = 0u, ntri = 0u;
+        if (cellsRow) {
+            cellm = ((S00 ^ S10) | (S00 ^ S11) | (S00 ^ S01) | (S00 ^ P00) | (S00 ^ P10) | (S00 ^ P11) |
+                     (S00 ^ P01)) & kc;
+            for (unsigned m = cellm; m; m &= m - 1u) {
+                unsigned b = __ffs(m) - 1;
+                ntri += (unsigned)(s_tab[cube_index(b, S00, S10, S11, S01, P00, P10, P11, P01)] >> 60);
+            }
+        }
+        if (!EMIT) {
+            triCarry += warp_sum(ntri);
+            ec0 += warp_sum(c00);
+            continue;
+        }
+        // Edges owned by the three neighbouring rows, for triangle corners.
+        const unsigned S20 = L(2, 0, w), S21 = L(2, 1, w), S02 = L(0, 2, w), S12 = L(1, 2, w);
+        const unsigned N20 = L(2, 0, w + 1), N21 = L(2, 1, w + 1), N02 = L(0, 2, w + 1), N12 = L(1, 2, w + 1);
+        const bool r1 = j + 1 <= Gc, r2 = i + 1 <= Gc, r3 = r1 && r2;
+        const unsigned X01 = (r1 && i < Gc) ? (S01 ^ S11) & kv : 0u;
+        const unsigned Y01 = (j + 1 < Gc) ? (S01 ^ S02) & kv : 0u;
+        const unsigned Z01 = r1 ? (S01 ^ P01) & kc : 0u;
+        const unsigned X10 = (i + 1 < Gc) ? (S10 ^ S20) & kv : 0u;
+        const unsigned Y10 = (r2 && j < Gc) ? (S10 ^ S11) & kv : 0u;
+        const unsigned Z10 = r2 ? (S10 ^ P10) & kc : 0u;
+        const unsigned X11 = (r1 && i + 1 < Gc) ? (S11 ^ S21) & kv : 0u;
+        const unsigned Y11 = (r2 && j + 1 < Gc) ? (S11 ^ S12) & kv : 0u;
+        const unsigned Z11 = r3 ? (S11 ^ P11) & kc : 0u;
+        const unsigned c01 = __popc(X01) + __popc(Y01) + __popc(Z01);
+        const unsigned c10 = __popc(X10) + __popc(Y10) + __popc(Z10);
+        const unsigned c11 = __popc(X11) + __popc(Y11) + __popc(Z11);
+        // Activity of the x/y edges of voxel kb+32 (bit 0 of the next word).
+        const unsigned xn0 = (nxt && i < Gc) ? ((N00 ^ N10) & 1u) : 0u, yn0 = (nxt && j < Gc) ? ((N00 ^ N01) & 1u) : 0u;
+        const unsigned xn1 = (nxt && r1 && i < Gc) ? ((N01 ^ N11) & 1u) : 0u, yn1 = (nxt && j + 1 < Gc) ? ((N01 ^ N02) & 1u) : 0u;
+        const unsigned xn2 = (nxt && i + 1 < Gc) ? ((N10 ^ N20) & 1u) : 0u, yn2 = (nxt && r2 && j < Gc) ? ((N10 ^ N11) & 1u) : 0u;
+        const unsigned xn3 = (nxt && r1 && i + 1 < Gc) ? ((N11 ^ N21) & 1u) : 0u, yn3 = (nxt && r2 && j + 1 < Gc) ? ((N11 ^ N12) & 1u) : 0u;
+
+        const unsigned p0 = warp_incl_scan(c00) - c00, p1 = warp_incl_scan(c01) - c01;
+        const unsigned p2 = warp_incl_scan(c10) - c10, p3 = warp_incl_scan(c11) - c11;
+        const unsigned tp = warp_incl_scan(ntri) - ntri;
+
+        // Vertices owned by this row, in voxel order, x then y then z within a voxel.
+        {
+            unsigned slot = eb0 + ec0 + p0;
+            for (unsigned m = X00 | Y00 | Z00; m; m &= m - 1u) {
+                const unsigned b = __ffs(m) - 1;
+                const int k = kb + (int)b;
+                if ((X00 >> b) & 1u) vkey[slot++] = edge_key(g, codes, s_lut, i, j, k, 0);
+                if ((Y00 >> b) & 1u) vkey[slot++] = edge_key(g, codes, s_lut, i, j, k, 1);
+                if ((Z00 >> b) & 1u) vkey[slot++] = edge_key(g, codes, s_lut, i, j, k, 2);
+            }
+        }
+        // Triangles in cell order, corners as pre-weld vertex slots.
+        {
+            unsigned ts = triBase + triCarry + tp;
+            for (unsigned m = cellm; m; m &= m - 1u) {
+                const unsigned b = __ffs(m) - 1;
+                const unsigned long long e = s_tab[cube_index(b, S00, S10, S11, S01, P00, P10, P11, P01)];
+                const unsigned nt = (unsigned)(e >> 60);
+                for (unsigned q = 0; q < 3 * nt; q++) {
+                    const unsigned edge = (unsigned)(e >> (4 * q)) & 15u;
+                    const unsigned own = (unsigned)(kEdgeOwner >> (5 * edge)) & 31u;
+                    const int o = (int)((own & 1u) * 2 + ((own >> 1) & 1u));  // (di, dj) -> owner index
+                    const unsigned dk = (own >> 2) & 1u, ax = own >> 3;
+                    const unsigned Xo = sel4(o, X00, X01, X10, X11), Yo = sel4(o, Y00, Y01, Y10, Y11);
+                    const unsigned Zo = sel4(o, Z00, Z01, Z10, Z11);
+                    unsigned slot = sel4(o, eb0 + ec0 + p0, eb1 + ec1 + p1, eb2 + ec2 + p2, eb3 + ec3 + p3);
+                    const unsigned vb = b + dk;
+                    if (vb < 32) {
+                        const unsigned lt = (1u << vb) - 1u;
+                        slot += __popc(Xo & lt) + __popc(Yo & lt) + __popc(Zo & lt);
+                        if (ax >= 1) slot += (Xo >> vb) & 1u;
+                        if (ax >= 2) slot += (Yo >> vb) & 1u;
+                    } else {
+                        slot += sel4(o, c00, c01, c10, c11);
+                        if (ax >= 1) slot += sel4(o, xn0, xn1, xn2, xn3);
+                        if (ax >= 2) slot += sel4(o, yn0, yn1, yn2, yn3);
+                    }
+                    tri[3ull * ts + q] = slot;
+                }
+                ts += nt;
+            }
+        }
+        triCarry += warp_sum(ntri);
+        ec0 += warp_sum(c00);
+        ec1 += warp_sum(c01);
+        ec2 += warp_sum(c10);
+        ec3 += warp_sum(c11);
+    }
+    if (!EMIT && lane == 0) rowCount[row] = make_uint2(triCarry, ec0);
+}
+
+// ------------------------------------------------------------------ weld
+
+__global__ void k_weld_flags(const unsigned long long *__restrict__ skey, unsigned n, uint2 *__restrict__ flags) {
+    unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    flags[p] = make_uint2((p == 0 || skey[p] != skey[p - 1]) ? 1u : 0u, 0u);
+}
+
+__global__ void k_weld_scatter(QGrid g, const unsigned long long *__restrict__ skey,
+                               const unsigned *__restrict__ sval, const uint2 *__restrict__ excl, unsigned n,
+                               unsigned *__restrict__ vmap, float *__restrict__ vq) {
+    unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const bool first = (p == 0 || skey[p] != skey[p - 1]);
+    const unsigned rank = excl[p].x + (first ? 1u : 0u) - 1u;
+    vmap[sval[p]] = rank;
+    if (first) {
+        const unsigned long long key = skey[p], R = (unsigned long long)g.Rq;
+        const long long mz = (long long)(key % R) + g.bz;
+        const long long my = (long long)((key / R) % R) + g.by;
+        const long long mx = (long long)(key / (R * R)) + g.bx;
+        vq[3ull * rank] = __fmul_rn((float)mx, QSES_WELD_TOL);
+        vq[3ull * rank + 1] = __fmul_rn((float)my, QSES_WELD_TOL);
+        vq[3ull * rank + 2] = __fmul_rn((float)mz, QSES_WELD_TOL);
+    }
+}
+
+__global__ void k_remap(unsigned *__restrict__ tri, size_t n3, const unsigned *__restrict__ vmap) {
+    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n3) tri[q] = vmap[tri[q]];
+}
+
+// ------------------------------------------------------------ closest atom
+
+__global__ void k_closest(QGrid g, const float *__restrict__ vq, unsigned nv, const float4 *__restrict__ atoms,
+                          const uint2 *__restrict__ cells, const unsigned *__restrict__ sorted_to_input,
+                          int *__restrict__ asorted, int *__restrict__ ainput) {
+    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const float qx = vq[3ull * v], qy = vq[3ull * v + 1], qz = vq[3ull * v + 2];
+    const int cx = __float2int_rz(__fdiv_rn(__fsub_rn(qx, g.ox), g.cell));
+    const int cy = __float2int_rz(__fdiv_rn(__fsub_rn(qy, g.oy), g.cell));
+    const int cz = __float2int_rz(__fdiv_rn(__fsub_rn(qz, g.oz), g.cell));
+    int best = -1;
+    float bestd = FLT_MAX;
+    for (int a = -1; a <= 1; a++) {
+        const int xx = min(max(cx + a, 0), g.gnb - 1);
+        for (int b = -1; b <= 1; b++) {
+            const int yy = min(max(cy + b, 0), g.gnb - 1);
+            for (int d = -1; d <= 1; d++) {
+                const int zz = min(max(cz + d, 0), g.gnb - 1);
+                const uint2 rg = cells[((size_t)xx * g.gnb + yy) * g.gnb + zz];
+                for (unsigned s = rg.x; s < rg.y; s++) {
+                    const float4 at = atoms[s];
+                    const float ex = __fsub_rn(at.x, qx), ey = __fsub_rn(at.y, qy), ez = __fsub_rn(at.z, qz);
+                    const float d2 = __fmaf_rn(ez, ez, __fmaf_rn(ey, ey, __fmul_rn(ex, ex)));
+                    if (d2 < bestd) {
+                        bestd = d2;
+                        best = (int)s;
+                    }
+                }
+            }
+        }
+    }
+    asorted[v] = best;
+    ainput[v] = best >= 0 ? (int)sorted_to_input[best] : -1;
+}
+
+// ------------------------------------------------------ degenerate filter
+
+__global__ void k_tri_flags(const unsigned *__restrict__ tri, unsigned nt, uint2 *__restrict__ flags) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const unsigned a = tri[3ull * t], b = tri[3ull * t + 1], c = tri[3ull * t + 2];
+    flags[t] = make_uint2((a != b && b != c && a != c) ? 1u : 0u, 0u);
+}
+
+__global__ void k_tri_compact(const unsigned *__restrict__ tri, unsigned nt, const uint2 *__restrict__ excl,
+                              unsigned *__restrict__ out) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const unsigned a = tri[3ull * t], b = tri[3ull * t + 1], c = tri[3ull * t + 2];
+    if (a != b && b != c && a != c) {
+        const size_t o = 3ull * excl[t].x;
+        out[o] = a; out[o + 1] = b; out[o + 2] = c;
+    }
+}
+
+// --------------------------------------------------------------- smoothing
+
+__global__ void k_degree(const unsigned *__restrict__ tri, size_t n3, unsigned nv, uint2 *__restrict__ deg) {
+    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n3) atomicAdd(&deg[tri[q]].x, 2u);
+}
+
+__global__ void k_copy_keys(const unsigned *__restrict__ tri, size_t n3, unsigned *__restrict__ keys) {
+    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n3) keys[q] = tri[q];
+}
+
+// Sorted occurrence p (vertex v, corner q = 3t + c in triangle order) contributes the two
+// other corners of triangle t to v's list, as getNeighboorsVertices appends them.
+__global__ void k_csr_fill(const unsigned *__restrict__ tri, const unsigned *__restrict__ socc, size_t n3,
+                           unsigned *__restrict__ nbr) {
+    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n3) return;
+    const unsigned q = socc[p], t = q / 3u, c = q - 3u * t;
+    const unsigned a = tri[3ull * t], b = tri[3ull * t + 1], d = tri[3ull * t + 2];
+    nbr[2 * p] = c == 0 ? b : a;
+    nbr[2 * p + 1] = c == 2 ? b : d;
+}
+
+__global__ void k_lower_count(const uint2 *__restrict__ start, const unsigned *__restrict__ nbr, unsigned nv,
+                              int *__restrict__ lower) {
+    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const unsigned e1 = v + 1 < nv ? start[v + 1].x : start[nv].x;
+    int c = 0;
+    for (unsigned e = start[v].x; e < e1; e++) c += nbr[e] < v;
+    lower[v] = c;
+}
+
+__global__ void k_gs_seed(const int *__restrict__ lower, int *__restrict__ cnt, unsigned nv,
+                          unsigned *__restrict__ queue, unsigned *__restrict__ qtail) {
+    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const int c = lower[v];
+    cnt[v] = c;
+    if (c == 0) queue[atomicAdd(qtail, 1u)] = v;
+}
+
+// One Gauss-Seidel pass.  Threads take queue slots in order; a slot is filled when its
+// vertex's last lower neighbour finishes, so every vertex reads final values for lower ids
+// and untouched values for higher ids, in its own neighbour-list order.  All waits are
+// bounded by `spin_cycles`.
+__global__ void __launch_bounds__(256) k_gs(float *pos, unsigned nv, const uint2 *__restrict__ start,
+                                            const unsigned *__restrict__ nbr, int *cnt, unsigned *queue,
+                                            unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles) {
+    for (;;) {
+        const unsigned idx = atomicAdd(qhead, 1u);
+        if (idx >= nv) return;
+        unsigned v = 0xffffffffu;
+        const long long t0 = clock64();
+        for (unsigned it = 0;; it++) {
+            v = ld_acquire_u32(&queue[idx]);
+            if (v != 0xffffffffu) break;
+            if ((it & 63u) == 63u && clock64() - t0 > spin_cycles) {
+                raise_error(err, QSES_ERR_TIMEOUT);
+                return;
+            }
+            __nanosleep(100);
+        }
+        if (v >= nv) {
+            raise_error(err, QSES_ERR_INTERNAL);
+            return;
+        }
+        const unsigned e0 = start[v].x, e1 = v + 1 < nv ? start[v + 1].x : start[nv].x;
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        for (unsigned e = e0; e < e1; e++) {
+            const unsigned u = nbr[e];
+            sx = __fadd_rn(sx, __ldcg(pos + 3ull * u));
+            sy = __fadd_rn(sy, __ldcg(pos + 3ull * u + 1));
+            sz = __fadd_rn(sz, __ldcg(pos + 3ull * u + 2));
+        }
+        const float n = (float)(int)(e1 - e0);
+        __stcg(pos + 3ull * v, __fdiv_rn(sx, n));
+        __stcg(pos + 3ull * v + 1, __fdiv_rn(sy, n));
+        __stcg(pos + 3ull * v + 2, __fdiv_rn(sz, n));
+        __threadfence();
+        for (unsigned e = e0; e < e1; e++) {
+            const unsigned u = nbr[e];
+            if (u > v && atomicSub(&cnt[u], 1) == 1) {
+                __threadfence();
+                const unsigned slot = atomicAdd(qtail, 1u);
+                if (slot < nv) st_release_u32(&queue[slot], u);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------ launchers
+
+static inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+void launch_mc_count(const QGrid &g, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
+    size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
+    k_mc<false><<<nblk(rows, 8), 256, 0, s>>>(g, sign, nullptr, nullptr, rowCount, nullptr, nullptr, nullptr);
+}
+void launch_mc_emit(const QGrid &g, const unsigned *sign, const unsigned char *codes, const float *lut,
+                    const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s) {
+    size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
+    k_mc<true><<<nblk(rows, 8), 256, 0, s>>>(g, sign, codes, lut, nullptr, rowBase, tri, vkey);
+}
+void launch_weld_flags(const unsigned long long *skey, unsigned n, uint2 *flags, cudaStream_t s) {
+    k_weld_flags<<<nblk(n, 256), 256, 0, s>>>(skey, n, flags);
+}
+void launch_weld_scatter(const QGrid &g, const unsigned long long *skey, const unsigned *sval, const uint2 *excl,
+                         unsigned n, unsigned *vmap, float *vq, cudaStream_t s) {
+    k_weld_scatter<<<nblk(n, 256), 256, 0, s>>>(g, skey, sval, excl, n, vmap, vq);
+}
+void launch_remap(unsigned *tri, size_t n3, const unsigned *vmap, cudaStream_t s) {
+    k_remap<<<nblk(n3, 256), 256, 0, s>>>(tri, n3, vmap);
+}
+void launch_closest(const QGrid &g, const float *vq, unsigned nv, const float4 *atoms, const uint2 *cells,
+                    const unsigned *sorted_to_input, int *asorted, int *ainput, cudaStream_t s) {
+    k_closest<<<nblk(nv, 128), 128, 0, s>>>(g, vq, nv, atoms, cells, sorted_to_input, asorted, ainput);
+}
+void launch_tri_flags(const unsigned *tri, unsigned nt, uint2 *flags, cudaStream_t s) {
+    k_tri_flags<<<nblk(nt, 256), 256, 0, s>>>(tri, nt, flags);
+}
+void launch_tri_compact(const unsigned *tri, unsigned nt, const uint2 *excl, unsigned *out, cudaStream_t s) {
+    k_tri_compact<<<nblk(nt, 256), 256, 0, s>>>(tri, nt, excl, out);
+}
+void launch_degree(const unsigned *tri, size_t n3, unsigned nv, uint2 *deg, cudaStream_t s) {
+    k_degree<<<nblk(n3, 256), 256, 0, s>>>(tri, n3, nv, deg);
+}
+void launch_copy_keys(const unsigned *tri, size_t n3, unsigned *keys, cudaStream_t s) {
+    k_copy_keys<<<nblk(n3, 256), 256, 0, s>>>(tri, n3, keys);
+}
+void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s) {
+    k_csr_fill<<<nblk(n3, 256), 256, 0, s>>>(tri, socc, n3, nbr);
+}
+void launch_lower_count(const uint2 *start, const unsigned *nbr, unsigned nv, int *lower, cudaStream_t s) {
+    k_lower_count<<<nblk(nv, 256), 256, 0, s>>>(start, nbr, nv, lower);
+}
+void launch_gs_seed(const int *lower, int *cnt, unsigned nv, unsigned *queue, unsigned *qtail, cudaStream_t s) {
+    k_gs_seed<<<nblk(nv, 256), 256, 0, s>>>(lower, cnt, nv, queue, qtail);
+}
+cudaError_t launch_gs(float *pos, unsigned nv, const uint2 *start, const unsigned *nbr, int *cnt, unsigned *queue,
+                      unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles, int blocks, cudaStream_t s) {
+    void *args[] = {&pos, &nv, (void *)&start, (void *)&nbr, &cnt, &queue, &qhead, &qtail, &err, &spin_cycles};
+    return cudaLaunchCooperativeKernel((const void *)k_gs, dim3(blocks), dim3(256), args, 0, s);
+}
+int gs_max_blocks(int device) {
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gs, 256, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    return per_sm * sms;
+}
+
+}  // namespace qses

@@ -1,0 +1,39 @@
+// Kernel launchers (host side).  Every launcher enqueues on the given stream only.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "qses_internal.h"
+
+namespace qses {
+
+void launch_atom_minmax(const float *xyz, const float *r, unsigned n, unsigned *mm, cudaStream_t s);
+void launch_atom_hash(const QGrid &g, const float *xyz, unsigned n, unsigned *key, cudaStream_t s);
+void launch_atom_gather(const float *xyz, const float *r, const unsigned *skey, const unsigned *sidx, unsigned n,
+                        float4 *atoms, uint2 *cells, cudaStream_t s);
+void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigned *inMask, unsigned *outMask,
+                cudaStream_t s);
+void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
+                unsigned *signMask, cudaStream_t s);
+
+void launch_mc_count(const QGrid &g, const unsigned *sign, uint2 *rowCount, cudaStream_t s);
+void launch_mc_emit(const QGrid &g, const unsigned *sign, const unsigned char *codes, const float *lut,
+                    const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s);
+void launch_weld_flags(const unsigned long long *skey, unsigned n, uint2 *flags, cudaStream_t s);
+void launch_weld_scatter(const QGrid &g, const unsigned long long *skey, const unsigned *sval, const uint2 *excl,
+                         unsigned n, unsigned *vmap, float *vq, cudaStream_t s);
+void launch_remap(unsigned *tri, size_t n3, const unsigned *vmap, cudaStream_t s);
+void launch_closest(const QGrid &g, const float *vq, unsigned nv, const float4 *atoms, const uint2 *cells,
+                    const unsigned *sorted_to_input, int *asorted, int *ainput, cudaStream_t s);
+void launch_tri_flags(const unsigned *tri, unsigned nt, uint2 *flags, cudaStream_t s);
+void launch_tri_compact(const unsigned *tri, unsigned nt, const uint2 *excl, unsigned *out, cudaStream_t s);
+void launch_degree(const unsigned *tri, size_t n3, unsigned nv, uint2 *deg, cudaStream_t s);
+void launch_copy_keys(const unsigned *tri, size_t n3, unsigned *keys, cudaStream_t s);
+void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s);
+void launch_lower_count(const uint2 *start, const unsigned *nbr, unsigned nv, int *lower, cudaStream_t s);
+void launch_gs_seed(const int *lower, int *cnt, unsigned nv, unsigned *queue, unsigned *qtail, cudaStream_t s);
+cudaError_t launch_gs(float *pos, unsigned nv, const uint2 *start, const unsigned *nbr, int *cnt, unsigned *queue,
+                      unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles, int blocks, cudaStream_t s);
+int gs_max_blocks(int device);
+
+}  // namespace qses

@@ -1,0 +1,123 @@
+"""GPU path vs the CPU oracle on seeded small molecules, through the C-ABI.
+
+Bar: bit-exact against the oracle's FP32 mode (same arithmetic order) for voxel codes,
+atom order, welded vertices, triangles and atom ids; against the FP64 oracle the mesh is
+within a symmetric Hausdorff distance of 0.05 voxel.
+"""
+import numpy as np
+import pytest
+
+import quickses_gb300 as q
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+HAUSDORFF_TOL = 0.05  # in voxels
+
+CASES = [
+    ("ball", 2, 3, 0.5), ("ball", 30, 1, 0.5), ("ball", 200, 2, 0.5), ("ball", 1000, 1, 0.5),
+    ("ball", 300, 4, 0.4), ("ball", 300, 5, 0.3), ("ball", 250, 6, 0.2), ("shell", 400, 9, 0.5),
+]
+
+
+def _atoms(kind, n, seed):
+    if kind == "ball":
+        xyz, rad, _ = q.molecules.ball(n, seed)
+    else:
+        xyz, rad, _ = q.molecules.shell(n, seed, r_in=12.0, thickness=4.0)
+    return xyz, rad
+
+
+def _compare_exact(m, ref, keep_degenerate=False):
+    assert m.vertices.shape == ref.vertices.shape
+    assert np.array_equal(m.vertices, ref.vertices.astype(np.float32))
+    tri_ref = ref.triangles if keep_degenerate else ref.triangles_kept
+    assert np.array_equal(m.triangles, tri_ref)
+    assert np.array_equal(m.atom_sorted, ref.atom_sorted)
+    assert np.array_equal(m.atom_input, ref.atom_input)
+
+
+@pytest.mark.parametrize("kind,n,seed,dx", CASES)
+def test_field_codes_exact(ctx, kind, n, seed, dx):
+    xyz, rad = _atoms(kind, n, seed)
+    ctx.compute(xyz, rad, voxel=dx, smooth=0)
+    g, _ = O.grid(xyz, rad, dx)
+    codes = ctx.debug_codes(g.G)
+    ref = O.field_codes(xyz, rad, g, fp64=False)
+    mism = np.argwhere(codes != ref)
+    assert len(mism) == 0, "first mismatches %s gpu=%s oracle=%s" % (
+        mism[:5].tolist(), codes[tuple(mism[:5].T)].tolist(), ref[tuple(mism[:5].T)].tolist())
+
+
+@pytest.mark.parametrize("kind,n,seed,dx", CASES)
+def test_atom_order_exact(ctx, kind, n, seed, dx):
+    xyz, rad = _atoms(kind, n, seed)
+    ctx.compute(xyz, rad, voxel=dx, smooth=0)
+    order, keys = ctx.debug_atom_order(n)
+    g, _ = O.grid(xyz, rad, dx)
+    ref_order, ref_hash = O.sort_atoms(xyz, g)
+    assert np.array_equal(order, ref_order)
+    assert np.array_equal(keys, ref_hash[ref_order].astype(np.uint32))
+
+
+@pytest.mark.parametrize("smooth", [0, 1, 3])
+@pytest.mark.parametrize("kind,n,seed,dx", CASES)
+def test_mesh_exact_fp32(ctx, kind, n, seed, dx, smooth):
+    xyz, rad = _atoms(kind, n, seed)
+    m = ctx.compute(xyz, rad, voxel=dx, smooth=smooth)
+    ref = O.compute_ses(xyz, rad, dx, smooth=smooth, fp64=False)
+    _compare_exact(m, ref)
+
+
+def test_keep_degenerate_exact(ctx):
+    xyz, rad = _atoms("ball", 250, 6)
+    m = ctx.compute(xyz, rad, voxel=0.2, smooth=1, keep_degenerate=True)
+    ref = O.compute_ses(xyz, rad, 0.2, smooth=1, fp64=False)
+    _compare_exact(m, ref, keep_degenerate=True)
+
+
+@pytest.mark.parametrize("kind,n,seed,dx", CASES[1:])
+def test_mesh_vs_fp64_hausdorff(ctx, kind, n, seed, dx):
+    xyz, rad = _atoms(kind, n, seed)
+    m = ctx.compute(xyz, rad, voxel=dx, smooth=1)
+    ref = O.compute_ses(xyz, rad, dx, smooth=1, fp64=True)
+    h, _, _ = O.hausdorff(m.vertices.astype(np.float64), m.triangles, ref.vertices, ref.triangles_kept)
+    assert h <= HAUSDORFF_TOL * dx, "Hausdorff %.4g A > %.4g A" % (h, HAUSDORFF_TOL * dx)
+    assert abs(len(m.vertices) - len(ref.vertices)) <= max(2, 0.01 * len(ref.vertices))
+
+
+def test_empty_inputs(ctx):
+    for n in (0, 1):
+        xyz = np.zeros((n, 3), np.float32)
+        rad = np.full(n, 1.7, np.float32)
+        m = ctx.compute(xyz, rad, voxel=0.5)
+        assert len(m.vertices) == 0 and len(m.triangles) == 0
+
+
+def test_coincident_atoms(ctx):
+    xyz = np.zeros((6, 3), np.float32)
+    rad = np.array([1.7, 1.55, 1.52, 1.8, 1.7, 1.7], np.float32)
+    m = ctx.compute(xyz, rad, voxel=0.5, smooth=1)
+    ref = O.compute_ses(xyz, rad, 0.5, smooth=1, fp64=False)
+    _compare_exact(m, ref)
+    assert len(m.triangles) > 0
+
+
+def test_reference_api_semantics():
+    xyz, rad = _atoms("ball", 200, 2)
+    api = q.ReferenceAPI()
+    nv, nidx = api.computeSES(0.5, xyz, rad, smooth=1)
+    ref = O.compute_ses(xyz, rad, 0.5, smooth=1, fp64=False)
+    assert nv == len(ref.vertices) and nidx == 3 * len(ref.triangles_kept)  # NTri counts indices
+    assert api.exported_counts() == (nv, nidx)
+    v = api.getVertices(nv)
+    assert np.array_equal(v, ref.vertices.astype(np.float32))
+    t = api.getTriangles(nidx).reshape(-1, 3)
+    assert np.array_equal(t, ref.triangles_kept)
+    tw = api.getTriangles(nidx, invert=True).reshape(-1, 3)  # swaps the first two, in place
+    assert np.array_equal(tw[:, [1, 0, 2]], ref.triangles_kept)
+    tb = api.getTriangles(nidx, invert=True).reshape(-1, 3)
+    assert np.array_equal(tb, ref.triangles_kept)
+    assert np.array_equal(api.getAtomIdPerVert(nv), ref.atom_sorted)
+    api.freeMesh()
+    assert api.exported_counts() == (0, 0)

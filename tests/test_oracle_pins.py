@@ -1,0 +1,148 @@
+"""Pins the CPU oracle to QuickSES's own code (CPU, no GPU needed).
+
+The reference ships no tests or fixtures, so the pins are (1) golden vectors produced by
+running the reference's host-callable functions (tests/golden/gen_ref_golden.py) and
+(2) the same functions run live from oracle/_ref/ when the reference checkout exists.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import quickses_gb300 as q
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = np.load(os.path.join(HERE, "golden", "ref_host.npz"))
+CASES = sorted({k.split("_")[0] for k in GOLDEN.files})
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_hash_matches_reference(case):
+    xyz, rad, dx = GOLDEN[case + "_xyz"], GOLDEN[case + "_rad"], float(GOLDEN[case + "_dx"])
+    g, _ = O.grid(xyz, rad, dx)
+    _, h = O.sort_atoms(xyz, g)
+    assert np.array_equal(h, GOLDEN[case + "_hash"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_sas_classification_matches_reference(case):
+    """computeInOrOut vs the oracle's FP32 classification at every computed voxel.  The
+    reference compares sqrt(d^2) < r - dx; the oracle compares d^2 against the squared,
+    float-rounded threshold: they may only differ on exact ties, of which these seeds
+    have none."""
+    xyz, rad, dx = GOLDEN[case + "_xyz"], GOLDEN[case + "_rad"], float(GOLDEN[case + "_dx"])
+    g, _ = O.grid(xyz, rad, dx)
+    codes = O.field_codes(xyz, rad, g, fp64=False)[:-1, :-1, :-1]
+    cls = np.where(codes == O.CODE_OUT, 0, np.where(codes == O.CODE_IN, 2, 1)).astype(np.int8)
+    ref = GOLDEN[case + "_class"]
+    assert cls.shape == ref.shape
+    assert int((cls != ref).sum()) == 0
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_smoothing_matches_reference_bitwise(case):
+    v, t = GOLDEN[case + "_mesh_v"], GOLDEN[case + "_mesh_t"]
+    out = O.smooth_f32(v, t, 1)
+    assert np.array_equal(out, GOLDEN[case + "_smooth1"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_closest_atom_matches_reference(case):
+    xyz, rad, dx = GOLDEN[case + "_xyz"], GOLDEN[case + "_rad"], float(GOLDEN[case + "_dx"])
+    m = O.compute_ses(xyz, rad, dx, smooth=0, fp64=False)
+    assert np.array_equal(m.vertices.astype(np.float32), GOLDEN[case + "_mesh_v"])
+    assert np.array_equal(m.atom_sorted, GOLDEN[case + "_closest"])
+
+
+def _ref_lib():
+    path = os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libqses_ref_host.so")
+    if not os.path.exists(path):
+        pytest.skip("reference checkout not available on this machine")
+    L = ctypes.CDLL(path)
+    L.ref_smooth.restype = None
+    L.ref_smooth.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint]
+    return L
+
+
+@pytest.mark.parametrize("passes", [1, 2, 3])
+def test_smoothing_live_reference_multipass(passes):
+    """The oracle's Gauss-Seidel pass against SmoothMesh.cpp itself on a fresh mesh,
+    including degenerate triangles (dx = 0.2 produces many)."""
+    L = _ref_lib()
+    xyz, rad, _ = q.molecules.ball(150, 21)
+    m = O.compute_ses(xyz, rad, 0.2, smooth=0, fp64=False)
+    v = m.vertices.astype(np.float32)
+    t = np.ascontiguousarray(m.triangles, np.int32)
+    assert (t[:, 0] == t[:, 1]).any() or (t[:, 1] == t[:, 2]).any() or (t[:, 0] == t[:, 2]).any()
+    ref = np.ascontiguousarray(v.copy())
+    L.ref_smooth(passes, ref.ctypes.data_as(ctypes.c_void_p), t.ctypes.data_as(ctypes.c_void_p), len(v), len(t))
+    assert np.array_equal(O.smooth_f32(v, t, passes), ref)
+
+
+def test_mc_tables_match_reference_source():
+    """The packed kernel table and the oracle table both equal MarchingCubes.cu:64-343."""
+    src = "/root/reference/MarchingCubes.cu"
+    root = os.path.dirname(HERE)
+    packed = open(os.path.join(root, "quickses_gb300", "csrc", "mc_tables.h")).read()
+    words = [int(x, 16) for x in re.findall(r"0x([0-9a-f]{16})ULL", packed)]
+    otab = open(os.path.join(root, "oracle", "mc_table.h")).read()
+    rows = [[int(v) for v in r.split(",")] for r in re.findall(r"\{([-\d, ]+)\}", otab)]
+    assert len(words) == 256 and len(rows) == 256
+    for c in range(256):
+        n = 0
+        while n < 16 and rows[c][n] != -1:
+            n += 1
+        assert (words[c] >> 60) * 3 == n
+        assert all(((words[c] >> (4 * v)) & 15) == rows[c][v] for v in range(n))
+        # every sign-changing edge of the case is used (welded vertices = active edges)
+        corners = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5), (2, 6), (3, 7)]
+        cross = {e for e, (a, b) in enumerate(corners) if ((c >> a) & 1) != ((c >> b) & 1)}
+        assert set(rows[c][:n]) == cross
+    if os.path.exists(src):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("g", os.path.join(root, "quickses_gb300", "csrc", "gen_mc_tables.py"))
+        gm = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(gm)
+        tri, nb = gm.load_reference(src)
+        assert tri == rows
+
+
+@pytest.mark.parametrize("n,seed,dx", [(80, 31, 0.5), (120, 32, 0.4), (90, 33, 0.2)])
+def test_oracle_fp32_vs_fp64(n, seed, dx):
+    """FP32 arithmetic vs FP64: identical voxel codes on these seeds, and the smoothed
+    meshes within 0.05 voxel (symmetric Hausdorff)."""
+    xyz, rad, _ = q.molecules.ball(n, seed)
+    g, _ = O.grid(xyz, rad, dx)
+    c32 = O.field_codes(xyz, rad, g, fp64=False)
+    c64 = O.field_codes(xyz, rad, g, fp64=True)
+    assert int((c32 != c64).sum()) == 0
+    l32, l64 = O.lut(g, False), O.lut(g, True)
+    assert np.all((l32 < 0) == (l64 < 0))
+    assert np.max(np.abs(l32.astype(np.float64) - l64)) < 1e-6
+    m32 = O.compute_ses(xyz, rad, dx, smooth=1, fp64=False)
+    m64 = O.compute_ses(xyz, rad, dx, smooth=1, fp64=True)
+    h, _, _ = O.hausdorff(m32.vertices, m32.triangles_kept, m64.vertices, m64.triangles_kept)
+    assert h <= 0.05 * dx
+
+
+def test_oracle_smoothing_is_sequential_gauss_seidel():
+    """Independent pure-Python statement of SmoothMesh.cpp's loop on a tiny mesh."""
+    xyz, rad, _ = q.molecules.ball(12, 41)
+    m = O.compute_ses(xyz, rad, 0.5, smooth=0, fp64=False)
+    v = m.vertices.astype(np.float32)
+    t = m.triangles
+    nb = [[] for _ in range(len(v))]
+    for a, b, c in t:
+        nb[a] += [b, c]
+        nb[b] += [a, c]
+        nb[c] += [a, b]
+    w = v.copy()
+    for i in range(len(w)):
+        s = np.zeros(3, np.float32)
+        for u in nb[i]:
+            s = (s + w[u]).astype(np.float32)
+        w[i] = (s / np.float32(len(nb[i]))).astype(np.float32)
+    assert np.array_equal(O.smooth_f32(v, t, 1), w)
