@@ -148,6 +148,13 @@ class Context:
     def last_launch_count(self):
         return int(self._lib.qses_last_launch_count(self._h))
 
+    def diagnostics(self):
+        out = (ctypes.c_ulonglong * 8)()
+        k = self._lib.qses_diagnostics(self._h, out, 8)
+        names = ["slabs", "slab_size", "max_polls", "unfinished_slabs", "update_cycles", "release_cycles",
+                 "vertices"]
+        return {names[q]: int(out[q]) for q in range(min(k, len(names)))}
+
 
 def grid_info(xyz, radii, voxel):
     xyz, radii = _f32(xyz, 3), _f32(radii)

@@ -230,6 +230,13 @@ QSES_API int qses_stage_times(qses_context *ctx, float *ms, const char **names, 
 
 QSES_API int qses_last_launch_count(qses_context *ctx) { return ctx ? ctx->launches : 0; }
 
+QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max) {
+    if (!ctx || !out) return 0;
+    int k = 0;
+    for (; k < max && k < 8; k++) out[k] = ctx->diag[k];
+    return k;
+}
+
 QSES_API int qses_grid_info_for(const qses_float3 *atoms, const float *radii, unsigned n, float voxel,
                                 qses_grid_info *out) {
     if (!atoms || !radii || !out || n == 0) return QSES_ERR_INVALID_ARG;

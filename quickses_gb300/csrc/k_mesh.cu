@@ -387,6 +387,265 @@ __global__ void __launch_bounds__(256) k_gs(float *pos, unsigned nv, const uint2
     }
 }
 
+// Slab-partitioned Gauss-Seidel pass.  Vertex ids are split into P contiguous slabs, one
+// persistent CTA each.  Every dependency edge goes from a lower to a higher id, so a chain
+// of updates crosses each slab boundary at most once: readiness inside a slab is tracked
+// with shared-memory counters and processed in rounds separated by __syncthreads, and only
+// boundary edges go through global memory (an acquire/release counter per vertex and a
+// per-slab inbox).  Each vertex is still computed exactly as the sequential loop would.
+constexpr int kGsT = 512;
+constexpr int kGsSlabMaxSmem = 200 * 1024;  // dynamic part: ring + packed counters, 6 B/vertex
+
+__device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(-v) : "memory");
+    return old;
+}
+
+// Per vertex: lower-id neighbour entries inside its slab (+1 if any lie in lower slabs),
+// and the count of entries in lower slabs.
+__global__ void k_gs_setup(const uint2 *__restrict__ start, const unsigned *__restrict__ nbr, unsigned nv,
+                           unsigned S, unsigned short *__restrict__ cnt_local, int *__restrict__ remote) {
+    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const unsigned lo = (v / S) * S;
+    unsigned loc = 0, rem = 0;
+    for (unsigned e = start[v].x; e < start[v + 1].x; e++) {
+        const unsigned u = nbr[e];
+        if (u < v) {
+            if (u >= lo) loc++; else rem++;
+        }
+    }
+    cnt_local[v] = (unsigned short)min(loc + (rem ? 1u : 0u), 65535u);
+    remote[v] = (int)rem;
+}
+
+// Gauss-Seidel update of one vertex.  Positions are float4 (one 16-byte load each); the
+// first 16 neighbour ids and their positions are all in flight before the in-order sum.
+// Padding lanes add +0.0f, which leaves a sum that started at +0.0f unchanged.
+__device__ __forceinline__ void gs_update4(unsigned v, unsigned e0, unsigned e1, const unsigned *__restrict__ nbr,
+                                           float4 *pos4, unsigned (&id)[16]) {
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    for (unsigned base = e0; base < e1; base += 16) {
+        const unsigned m = min(16u, e1 - base);
+#pragma unroll
+        for (unsigned q = 0; q < 16; q++) id[q] = __ldg(nbr + base + (q < m ? q : 0u));
+        float4 pq[16];
+#pragma unroll
+        for (unsigned q = 0; q < 16; q++) pq[q] = __ldcg(pos4 + id[q]);
+#pragma unroll
+        for (unsigned q = 0; q < 16; q++) {
+            sx = __fadd_rn(sx, q < m ? pq[q].x : 0.0f);
+            sy = __fadd_rn(sy, q < m ? pq[q].y : 0.0f);
+            sz = __fadd_rn(sz, q < m ? pq[q].z : 0.0f);
+        }
+    }
+    const float n = (float)(int)(e1 - e0);
+    __stcg(pos4 + v, make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f));
+}
+
+__global__ void k_to_float4(const float *__restrict__ v3, unsigned nv, float4 *__restrict__ v4) {
+    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < nv) v4[v] = make_float4(v3[3ull * v], v3[3ull * v + 1], v3[3ull * v + 2], 0.0f);
+}
+__global__ void k_from_float4(const float4 *__restrict__ v4, unsigned nv, float *__restrict__ v3) {
+    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < nv) {
+        const float4 q = v4[v];
+        v3[3ull * v] = q.x; v3[3ull * v + 1] = q.y; v3[3ull * v + 2] = q.z;
+    }
+}
+
+// Two 16-bit readiness counters per shared word; returns the counter value before the
+// decrement.  Counters never go below zero, so no borrow crosses into the other half.
+__device__ __forceinline__ unsigned dec16(unsigned *w, unsigned k) {
+    const unsigned sh = 16u * (k & 1u);
+    return (atomicSub(&w[k >> 1], 1u << sh) >> sh) & 0xffffu;
+}
+
+__device__ __forceinline__ void ring_push16(volatile unsigned short *ring, unsigned *tail, unsigned off) {
+    const unsigned k = atomicAdd(tail, 1u);
+    ring[k] = (unsigned short)off;  // each vertex enters the ring once: no wrap-around
+}
+
+__global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned nv, unsigned S,
+                                                  const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
+                                                  const unsigned short *__restrict__ cnt_local, int *remote,
+                                                  unsigned *inbox, unsigned *inbox_tail, int *err,
+                                                  long long spin_cycles, unsigned long long *stats) {
+    extern __shared__ unsigned s_dyn[];
+    __shared__ unsigned s_head, s_tail, s_done, s_seen, s_stop;
+    const unsigned p = blockIdx.x, a = p * S;
+    if (a >= nv) return;  // uniform per CTA
+    const unsigned b = min(a + S, nv), len = b - a;
+    unsigned *st = s_dyn;                                        // len + 1 CSR offsets of the slab
+    unsigned *cnt = s_dyn + (S + 1);                             // (len + 1) / 2 words: packed counters
+    volatile unsigned short *ring = (volatile unsigned short *)(cnt + (S + 1) / 2);  // slab offsets
+    unsigned *box = inbox + a;                                   // boundary arrivals from lower slabs
+    if (threadIdx.x == 0) { s_head = 0; s_tail = 0; s_done = 0; s_seen = 0; s_stop = 0; }
+    for (unsigned k = threadIdx.x; k <= len; k += kGsT) st[k] = start[a + k].x;
+    for (unsigned k = threadIdx.x; k < len; k += kGsT) ring[k] = 0xffffu;
+    for (unsigned k = threadIdx.x; 2 * k < len; k += kGsT) {
+        const unsigned lo = cnt_local[a + 2 * k], hi = 2 * k + 1 < len ? cnt_local[a + 2 * k + 1] : 0u;
+        cnt[k] = lo | (hi << 16);
+    }
+    __syncthreads();
+    for (unsigned k = threadIdx.x; k < len; k += kGsT)
+        if (cnt_local[a + k] == 0) ring_push16(ring, &s_tail, k);
+    __syncthreads();
+
+    const unsigned lane = threadIdx.x & 31;
+    unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0;
+    if (threadIdx.x < 32) {
+        // Warp 0 only takes boundary arrivals (the last lower-slab dependency of a vertex
+        // finished); it never updates vertices, so arrivals are never stuck behind a chain.
+        if (lane == 0) {
+            unsigned seen = 0, done_seen = 0;
+            long long last = clock64();
+            for (;;) {
+                if (*(volatile unsigned *)&s_done >= len || *(volatile unsigned *)&s_stop) break;
+                const unsigned tail = min(ld_acquire_u32(inbox_tail + p), len);
+                polls++;
+                for (unsigned k = seen; k < tail; k++) {
+                    unsigned u = 0xffffffffu;
+                    for (unsigned it = 0; it < (1u << 20) && u == 0xffffffffu; it++) u = ld_acquire_u32(box + k);
+                    if (u < a || u >= b) {
+                        raise_error(err, u == 0xffffffffu ? QSES_ERR_TIMEOUT : QSES_ERR_INTERNAL);
+                        s_stop = 1;
+                        break;
+                    }
+                    __threadfence_block();
+                    if (dec16(cnt, u - a) == 1u) ring_push16(ring, &s_tail, u - a);
+                }
+                const long long now = clock64();
+                const unsigned d = *(volatile unsigned *)&s_done;
+                if (tail != seen || d != done_seen) last = now;
+                seen = tail;
+                done_seen = d;
+                if (now - last > spin_cycles) {
+                    raise_error(err, QSES_ERR_TIMEOUT);
+                    s_stop = 1;
+                }
+                if (tail == seen) __nanosleep(20);
+            }
+        }
+    } else {
+        // Worker warps: one vertex per warp; lanes fetch neighbours in parallel.
+        for (;;) {
+            unsigned v = 0xffffffffu, quit = 0;
+            if (lane == 0) {
+                const unsigned h = *(volatile unsigned *)&s_head, t = *(volatile unsigned *)&s_tail;
+                if (h < t && atomicCAS(&s_head, h, h + 1) == h) {
+                    unsigned off = 0xffffu;
+                    for (unsigned it = 0; it < (1u << 20) && off == 0xffffu; it++) off = ring[h];  // reserved slot
+                    if (off == 0xffffu) {
+                        raise_error(err, QSES_ERR_TIMEOUT);
+                        s_stop = 1;
+                    } else {
+                        v = a + off;
+                    }
+                } else if (h >= t) {
+                    quit = (*(volatile unsigned *)&s_done >= len) || *(volatile unsigned *)&s_stop;
+                }
+            }
+            v = __shfl_sync(0xffffffffu, v, 0);
+            quit = __shfl_sync(0xffffffffu, quit, 0);
+            if (quit) break;
+            if (v == 0xffffffffu) {
+                __nanosleep(20);
+                continue;
+            }
+            while (v != 0xffffffffu) {  // follow the chain of vertices this warp releases
+                __threadfence_block();
+                const long long c0 = clock64();
+                const unsigned e0 = st[v - a], e1 = st[v - a + 1];
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                unsigned first_id = v;
+                for (unsigned base = e0; base < e1; base += 32) {
+                    const unsigned m = min(32u, e1 - base);
+                    const unsigned id = lane < m ? __ldg(nbr + base + lane) : v;
+                    if (base == e0) first_id = id;
+                    const float4 q = __ldcg(pos4 + id);
+                    // strictly in neighbour-list order; lanes past m add +0.0f (a sum that
+                    // started at +0.0f is unchanged by it)
+                    const float qx = lane < m ? q.x : 0.0f, qy = lane < m ? q.y : 0.0f, qz = lane < m ? q.z : 0.0f;
+#pragma unroll
+                    for (unsigned k = 0; k < 16; k++) {
+                        sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
+                        sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
+                        sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
+                    }
+                    if (m > 16) {
+#pragma unroll
+                        for (unsigned k = 16; k < 32; k++) {
+                            sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
+                            sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
+                            sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
+                        }
+                    }
+                }
+                const float n = (float)(int)(e1 - e0);
+                if (lane == 0) __stcg(pos4 + v, make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f));
+                const long long c1 = clock64();
+                // The new position must be visible before any successor can start: CTA scope
+                // inside the slab, GPU scope when a hand-off to a higher slab may follow.
+                const unsigned m0 = min(32u, e1 - e0);
+                const bool remote_any = __any_sync(0xffffffffu, lane < m0 && first_id > v && first_id >= b) ||
+                                        (e1 - e0 > 32);
+                if (lane == 0) {
+                    if (remote_any) __threadfence();
+                    else __threadfence_block();
+                }
+                __syncwarp();
+                // Release: one lane per neighbour entry.
+                unsigned next = 0xffffffffu;
+                for (unsigned base = e0; base < e1; base += 32) {
+                    const unsigned m = min(32u, e1 - base);
+                    const unsigned u = lane < m ? (base == e0 ? first_id : __ldg(nbr + base + lane)) : 0u;
+                    const bool higher = lane < m && u > v;
+                    const bool remote_edge = higher && u >= b;
+                    bool ready = false;
+                    if (higher) {
+                        if (!remote_edge) {
+                            ready = dec16(cnt, u - a) == 1u;
+                        } else if (atom_sub_acq_rel(remote + u, 1) == 1) {
+                            // last lower-slab dependency of u: hand u to its slab
+                            const unsigned qs = u / S;
+                            const unsigned k = atomicAdd(inbox_tail + qs, 1u);
+                            if (k < S) st_release_u32(inbox + (size_t)qs * S + k, u);
+                        }
+                    }
+                    unsigned mask = __ballot_sync(0xffffffffu, ready);
+                    if (mask && next == 0xffffffffu) {
+                        const unsigned f = __ffs(mask) - 1;
+                        next = __shfl_sync(0xffffffffu, u, f);  // continue with it directly
+                        mask &= ~(1u << f);
+                    }
+                    if ((mask >> lane) & 1u) ring_push16(ring, &s_tail, u - a);
+                }
+                if (lane == 0) atomicAdd(&s_done, 1u);
+                v = next;
+                const long long c2 = clock64();
+                cyc_update += c1 - c0;
+                cyc_release += c2 - c1;
+                nproc++;
+            }
+        }
+    }
+    __syncthreads();
+    if (stats) {  // diagnostics: polls (max), unfinished slabs, update cycles, release cycles, vertices
+        if (threadIdx.x == 0) {
+            atomicMax(stats, polls);
+            if (s_done < len) atomicAdd(stats + 1, 1ull);
+        }
+        if (lane == 0 && nproc) {
+            atomicAdd(stats + 2, cyc_update);
+            atomicAdd(stats + 3, cyc_release);
+            atomicAdd(stats + 4, nproc);
+        }
+    }
+}
+
 // ------------------------------------------------------------ launchers
 
 static inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
@@ -439,6 +698,35 @@ cudaError_t launch_gs(float *pos, unsigned nv, const uint2 *start, const unsigne
                       unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles, int blocks, cudaStream_t s) {
     void *args[] = {&pos, &nv, (void *)&start, (void *)&nbr, &cnt, &queue, &qhead, &qtail, &err, &spin_cycles};
     return cudaLaunchCooperativeKernel((const void *)k_gs, dim3(blocks), dim3(256), args, 0, s);
+}
+void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned nv, unsigned S, unsigned short *cnt_local,
+                     int *remote, cudaStream_t s) {
+    k_gs_setup<<<nblk(nv, 256), 256, 0, s>>>(start, nbr, nv, S, cnt_local, remote);
+}
+size_t gs_slab_smem(unsigned S) { return 4ull * (S + 1) + 4ull * ((S + 1) / 2) + 2ull * S + 16; }
+void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s) {
+    k_to_float4<<<nblk(nv, 256), 256, 0, s>>>(v3, nv, v4);
+}
+void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s) {
+    k_from_float4<<<nblk(nv, 256), 256, 0, s>>>(v4, nv, v3);
+}
+cudaError_t launch_gs_slab(float4 *pos, unsigned nv, unsigned S, int P, const uint2 *start, const unsigned *nbr,
+                           const unsigned short *cnt_local, int *remote, unsigned *glist, unsigned *inbox,
+                           unsigned *inbox_tail, int *err, long long spin_cycles, unsigned long long *stats,
+                           cudaStream_t s) {
+    (void)glist;
+    size_t smem = gs_slab_smem(S);
+    cudaFuncSetAttribute((const void *)k_gs_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
+    void *args[] = {&pos, &nv, &S, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
+                    &inbox_tail, &err, &spin_cycles, &stats};
+    return cudaLaunchCooperativeKernel((const void *)k_gs_flow, dim3(P), dim3(kGsT), args, smem, s);
+}
+int gs_slab_max_blocks(int device, unsigned S) {
+    cudaFuncSetAttribute((const void *)k_gs_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gs_flow, kGsT, gs_slab_smem(S));
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    return per_sm * sms;
 }
 int gs_max_blocks(int device) {
     int per_sm = 0, sms = 0;

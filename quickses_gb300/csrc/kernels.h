@@ -35,5 +35,16 @@ void launch_gs_seed(const int *lower, int *cnt, unsigned nv, unsigned *queue, un
 cudaError_t launch_gs(float *pos, unsigned nv, const uint2 *start, const unsigned *nbr, int *cnt, unsigned *queue,
                       unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles, int blocks, cudaStream_t s);
 int gs_max_blocks(int device);
+void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned nv, unsigned S, unsigned short *cnt_local,
+                     int *remote, cudaStream_t s);
+size_t gs_slab_smem(unsigned S);
+void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s);
+void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s);
+cudaError_t launch_gs_slab(float4 *pos, unsigned nv, unsigned S, int P, const uint2 *start, const unsigned *nbr,
+                           const unsigned short *cnt_local, int *remote, unsigned *glist, unsigned *inbox,
+                           unsigned *inbox_tail, int *err, long long spin_cycles, unsigned long long *stats,
+                           cudaStream_t s);
+int gs_slab_max_blocks(int device, unsigned S);
+constexpr unsigned kGsSlabMaxVerts = 25000;  // 8 B of shared memory per vertex, 16-bit slab offsets
 
 }  // namespace qses

@@ -159,6 +159,8 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     ctx->marks.clear();
     ctx->mesh = DeviceMesh();
     ctx->have_grid = false;
+    memset(ctx->diag, 0, sizeof(ctx->diag));
+    QCHK(cudaMemsetAsync((char *)ctx->small + 256, 0, 64, ctx->stream));
     ctx->mark("start");
 
     // ---- bounds (one read-back) and sizing on the host
@@ -260,7 +262,9 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     const size_t nflag = std::max<size_t>((size_t)NE + 1, (size_t)T) + 1;
     size_t needB = 2 * align256(4 * n3) + 2 * align256(8ull * NE) + 2 * align256(4ull * NE) + align256(8ull * nflag) +
                    align256(4ull * NE) + align256(12ull * NE) + 2 * align256(4ull * NE) + 2 * align256(4 * n3) +
-                   2 * align256(4 * n3) + align256(8 * n3) + 3 * align256(4ull * NE) + align256(tmpB) + 4096;
+                   2 * align256(4 * n3) + align256(8 * n3) + 3 * align256(4ull * NE) + align256(4ull * NE + 4096) + 4096 +
+                   align256(16ull * NE + 16) +
+                   align256(tmpB) + 4096;
     if (ctx->mesh_ws.reserve(needB) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "mesh workspace");
     Arena &B = ctx->mesh_ws;
     unsigned *tri = (unsigned *)B.take(4 * n3 + 4);
@@ -276,6 +280,9 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     unsigned *nbr = (unsigned *)B.take(8 * n3 + 8);
     int *lower = (int *)B.take(4ull * NE + 4), *cnt = (int *)B.take(4ull * NE + 4);
     unsigned *queue = (unsigned *)B.take(4ull * NE + 4);
+    unsigned *inbox = (unsigned *)B.take(4ull * NE + 4096);
+    unsigned *inbox_tail = (unsigned *)B.take(4096);
+    float4 *pos4 = (float4 *)B.take(16ull * NE + 16);
     void *tmpb = B.take(tmpB);
     if (!tmpb) return ctx->fail(QSES_ERR_INTERNAL, "mesh workspace layout");
 
@@ -325,17 +332,48 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         unsigned *socc = alt ? oval2 : oval;
         launch_csr_fill(tri, socc, n3, nbr, s);
         ctx->launches++;
-        launch_lower_count(deg, nbr, nv, lower, s);
-        ctx->launches++;
-        unsigned *qctl = (unsigned *)((char *)ctx->small + 128);
-        int blocks = std::min(ctx->gs_blocks, 64);
-        for (int pass = 0; pass < p.smooth_passes; pass++) {
-            QCHK(cudaMemsetAsync(queue, 0xff, 4ull * nv, s));
-            QCHK(cudaMemsetAsync(qctl, 0, 8, s));
-            launch_gs_seed(lower, cnt, nv, queue, qctl + 1, s);
+        ctx->mark("smooth_csr");
+        // Slab-partitioned exact Gauss-Seidel: P persistent CTAs, contiguous id slabs of S.
+        const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts), 1024);
+        int P = (int)std::min<unsigned>((nv + 16383) / 16384, (unsigned)pmax);
+        if (P < 1) P = 1;
+        unsigned S = (nv + P - 1) / P;
+        if (S > kGsSlabMaxVerts) {
+            P = (int)((nv + kGsSlabMaxVerts - 1) / kGsSlabMaxVerts);
+            S = (nv + P - 1) / P;
+        }
+        if (P <= pmax) {
+            launch_to_float4(vq, nv, pos4, s);
             ctx->launches++;
-            QCHK(launch_gs(vq, nv, deg, nbr, cnt, queue, qctl, qctl + 1, d_err, 4000000000ll, blocks, s));
+            for (int pass = 0; pass < p.smooth_passes; pass++) {
+                launch_gs_setup(deg, nbr, nv, S, (unsigned short *)cnt, lower, s);
+                ctx->launches++;
+                QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * P * S, s));
+                QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
+                unsigned long long *stats = (unsigned long long *)((char *)ctx->small + 256);
+                QCHK(cudaMemsetAsync(stats, 0, 64, s));
+                QCHK(launch_gs_slab(pos4, nv, S, P, deg, nbr, (unsigned short *)cnt, lower, queue, inbox, inbox_tail,
+                                    d_err, 4000000000ll, stats, s));
+                ctx->diag[0] = P;
+                ctx->diag[1] = S;
+                ctx->launches++;
+            }
+            launch_from_float4(pos4, nv, vq, s);
             ctx->launches++;
+        } else {
+            // Very large meshes: global-memory dataflow (same arithmetic, slower hand-offs).
+            launch_lower_count(deg, nbr, nv, lower, s);
+            ctx->launches++;
+            unsigned *qctl = (unsigned *)((char *)ctx->small + 128);
+            int blocks = std::min(ctx->gs_blocks, 64);
+            for (int pass = 0; pass < p.smooth_passes; pass++) {
+                QCHK(cudaMemsetAsync(queue, 0xff, 4ull * nv, s));
+                QCHK(cudaMemsetAsync(qctl, 0, 8, s));
+                launch_gs_seed(lower, cnt, nv, queue, qctl + 1, s);
+                ctx->launches++;
+                QCHK(launch_gs(vq, nv, deg, nbr, cnt, queue, qctl, qctl + 1, d_err, 4000000000ll, blocks, s));
+                ctx->launches++;
+            }
         }
     }
     ctx->mark("smooth");
@@ -352,8 +390,10 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         QCHK(cudaMemcpyAsync(ctx->h_small, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
     }
     QCHK(cudaMemcpyAsync(ctx->h_small + 8, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    QCHK(cudaMemcpyAsync(ctx->h_small + 2048, (char *)ctx->small + 256, 64, cudaMemcpyDeviceToHost, s));
     QCHK(cudaStreamSynchronize(s));
     ctx->mark("filter");
+    memcpy(ctx->diag + 2, ctx->h_small + 2048, 5 * sizeof(unsigned long long));
     if (!keep_all && T > 0) {
         memcpy(&tot, ctx->h_small, sizeof(tot));
         nkept = tot.x;

@@ -53,6 +53,7 @@ struct qses_context {
     std::vector<std::pair<const char *, cudaEvent_t>> marks;
     std::vector<std::pair<const char *, float>> times;
     int launches = 0;
+    unsigned long long diag[8] = {0};  // smoothing diagnostics: slabs, slab size, max/idle/total rounds
 
     int fail(int code, const char *what, cudaError_t e = cudaSuccess);
     void mark(const char *name);

@@ -1,0 +1,69 @@
+"""Full-size checks on the 50 000-atom / 0.2 A workload (grid 664^3, ~3.5 M vertices).
+
+The oracle cannot afford the whole field at this size, so the checks are split:
+* field: oracle codes on x-slabs (with their refine halo) == GPU codes there
+* mesh:  the oracle's marching cubes + weld + closest atom fed the GPU's field == GPU mesh
+* smoothing: the oracle's Gauss-Seidel pass on the GPU's unsmoothed mesh == GPU pass
+  (this exercises the slab-partitioned kernel with ~150 slabs)
+* size-independent properties: lexicographic vertex order, index ranges, no unused vertex
+"""
+import numpy as np
+import pytest
+
+import quickses_gb300 as q
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+WL = q.molecules.WORKLOADS["ball50k"]
+
+
+@pytest.fixture(scope="module")
+def big():
+    xyz, rad, _ = WL.atoms()
+    g, _ = O.grid(xyz, rad, WL.voxel)
+    with q.Context(0) as c:
+        m0 = c.compute(xyz, rad, voxel=WL.voxel, smooth=0, keep_degenerate=True)
+        codes = c.debug_codes(g.G)
+        m1 = c.compute(xyz, rad, voxel=WL.voxel, smooth=1, keep_degenerate=True)
+        m1k = c.compute(xyz, rad, voxel=WL.voxel, smooth=1, keep_degenerate=False)
+    return xyz, rad, g, m0, codes, m1, m1k
+
+
+@pytest.mark.parametrize("x0", [0, 200, 330, 640])
+def test_field_slab_exact(big, x0):
+    xyz, rad, g, _, codes, _, _ = big
+    x1 = min(x0 + 4, g.G)
+    ref = O.field_codes(xyz, rad, g, fp64=False, x0=x0, x1=x1)
+    assert np.array_equal(codes[x0:x1], ref)
+
+
+def test_mesh_from_gpu_field_exact(big):
+    xyz, rad, g, m0, codes, _, _ = big
+    ref = O.mesh_from_codes(codes, g, xyz, fp64=False, smooth=0)
+    assert np.array_equal(m0.vertices, ref.vertices.astype(np.float32))
+    assert np.array_equal(m0.triangles, ref.triangles)
+    assert np.array_equal(m0.atom_sorted, ref.atom_sorted)
+    assert np.array_equal(m0.atom_input, ref.atom_input)
+
+
+def test_smoothing_at_scale_exact(big):
+    _, _, _, m0, _, m1, _ = big
+    ref = O.smooth_f32(m0.vertices, m0.triangles, 1)
+    assert np.array_equal(m1.vertices, ref)
+    assert np.array_equal(m1.triangles, m0.triangles)
+
+
+def test_mesh_properties(big):
+    _, _, g, m0, _, _, m1k = big
+    v = m0.vertices.astype(np.float64)
+    # welded vertices are in strictly increasing lexicographic (x, y, z) order
+    d = np.diff(v, axis=0)
+    lex = (d[:, 0] > 0) | ((d[:, 0] == 0) & ((d[:, 1] > 0) | ((d[:, 1] == 0) & (d[:, 2] > 0))))
+    assert lex.all()
+    t = m0.triangles
+    assert t.min() >= 0 and t.max() < len(v)
+    assert np.bincount(t.ravel(), minlength=len(v)).min() > 0  # every vertex is used
+    tk = m1k.triangles
+    assert (tk[:, 0] != tk[:, 1]).all() and (tk[:, 1] != tk[:, 2]).all() and (tk[:, 0] != tk[:, 2]).all()
+    assert len(tk) < len(t)  # dx = 0.2 produces degenerate triangles, which the API drops
