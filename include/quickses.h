@@ -150,6 +150,25 @@ QSES_API int qses_last_launch_count(qses_context *ctx);
  * Returns the number of values written. */
 QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max);
 
+/* ------------------------------------------------------- allocation-free field */
+
+/* No counterpart in the reference.  For callers that must not allocate GPU memory while
+ * they run (plugins whose host application owns every device allocation, real-time loops
+ * that cannot afford cudaMalloc's implicit synchronisation, fixed memory budgets).
+ * Computes the SES voxel codes of one molecule - the same bytes qses_debug_codes returns
+ * after qses_compute - from device atoms (3n floats) and radii (n floats) into the caller's
+ * device buffer d_codes (G*G*G bytes, x-major, z fastest; G from qses_grid_info_for), on
+ * `cuda_stream` (NULL = legacy default stream).  Allocates nothing: its working memory is a
+ * fixed ~3.5 MB array inside the library, reserved on every GPU that loads the library
+ * until the process exits.  Limits: 2 <= n <= 4096 atoms, grid <= 128 voxels and <= 40
+ * neighbour cells per axis; larger inputs return QSES_ERR_UNSUPPORTED before any GPU
+ * work.  The first call on a device looks up the array's device address (make it before
+ * any stream capture).  All calls share the array: the function serialises host threads
+ * and waits for its own GPU work before returning; work that overlapped it on the GPU
+ * would race on the array. */
+QSES_API int qses_field_codes_noalloc(const float *d_xyz, const float *d_radii, unsigned n, float voxel,
+                                      uint8_t *d_codes, size_t codes_bytes, void *cuda_stream);
+
 /* --------------------------------------------------- inspection (tests, tooling) */
 
 typedef struct {

@@ -72,6 +72,8 @@ SIGNATURES = {
     "qses_stage_times": (ctypes.c_int, [_VP, _FP, ctypes.POINTER(ctypes.c_char_p), ctypes.c_int]),
     "qses_last_launch_count": (ctypes.c_int, [_VP]),
     "qses_diagnostics": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
+    "qses_field_codes_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_uint, ctypes.c_float, _VP, ctypes.c_size_t,
+                                                _VP]),
     "qses_grid_info_for": (ctypes.c_int, [_VP, _FP, ctypes.c_uint, ctypes.c_float, ctypes.POINTER(GridInfo)]),
     "qses_debug_codes": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t]),
     "qses_debug_atom_order": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
