@@ -238,12 +238,27 @@ def run_gpu(args):
         print(json.dumps(result))
 
 
+def run_once(args):
+    """One pipeline run through the C-ABI (host atoms in, host mesh out): a short program
+    for profiler captures, with few launches before the kernel of interest."""
+    import quickses_gb300 as q
+    wl = q.molecules.WORKLOADS[args.workload]
+    xyz, rad, _ = wl.atoms()
+    with q.Context(0) as ctx:
+        m = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=wl.smooth)
+        print(json.dumps({"workload": wl.name, "grid": q.grid_info(xyz, rad, wl.voxel).G,
+                          "vertices": len(m.vertices), "triangles": len(m.triangles),
+                          "launches": ctx.last_launch_count()}))
+
+
 def cpu_baseline(wl, xyz, rad, planes):
-    """The CPU oracle (FP32 mode, all host threads) on a central slab of the grid: SAS
-    classification + probe refine for `planes` x-planes (the refine halo is included in
-    the work).  voxels/s = slab voxels / time."""
+    """The CPU oracle (FP32 mode, all host threads): SAS classification + probe refine for
+    `planes` x-planes of the grid (default: all of them; the refine halo is included in the
+    work).  Marching cubes, weld and smoothing are left out, so this overstates the CPU's
+    end-to-end rate.  voxels/s = voxels covered / time."""
     from oracle import oracle as O
     g, _ = O.grid(xyz, rad, wl.voxel)
+    planes = g.G if planes <= 0 or planes > g.G else planes
     x0 = g.G // 2 - planes // 2
     t0 = time.perf_counter()
     O.field_codes(xyz, rad, g, fp64=False, x0=x0, x1=x0 + planes)
@@ -263,7 +278,7 @@ def run_reference(args):
     wl = q.molecules.WORKLOADS[args.workload]
     xyz, rad, _ = wl.atoms()
     g, _ = O.grid(xyz, rad, wl.voxel)
-    planes = args.cpu_planes
+    planes = g.G if args.cpu_planes <= 0 or args.cpu_planes > g.G else args.cpu_planes
     x0 = g.G // 2 - planes // 2
     times = []
     for it in range(args.warmup + args.steps):
@@ -293,12 +308,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ball50k")
-    ap.add_argument("--cpu-planes", type=int, default=192)
+    ap.add_argument("--cpu-planes", type=int, default=0, help="x-planes of the CPU sample (0 = whole grid)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="run the pipeline once on the workload (for profiler captures) and exit")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.profile_once:
+        run_once(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

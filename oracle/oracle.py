@@ -75,6 +75,8 @@ def lib():
         L.oracle_hausdorff.argtypes = [dp, ctypes.c_uint, ip, ctypes.c_uint, dp, ctypes.c_uint, ip, ctypes.c_uint,
                                        dp, dp, ctypes.c_int]
         L.oracle_hausdorff.restype = ctypes.c_double
+        L.oracle_point_surface.argtypes = [dp, ctypes.c_uint, dp, ctypes.c_uint, ip, ctypes.c_uint, dp, ctypes.c_int]
+        L.oracle_point_surface.restype = ctypes.c_double
         L.oracle_smooth_depth.argtypes = [ip, ctypes.c_uint, ctypes.c_uint, ip]
         L.oracle_smooth_depth.restype = ctypes.c_int
         _lib = L
@@ -174,6 +176,16 @@ def hausdorff(va, ta, vb, tb, threads=0):
                                _ptr(vb, ctypes.c_double), vb.shape[0], _ptr(tb, ctypes.c_int32), tb.shape[0],
                                ctypes.byref(ab), ctypes.byref(ba), threads)
     return h, ab.value, ba.value
+
+
+def point_surface(va, vb, tb, threads=0):
+    """Distance from every point of va to the triangle surface (vb, tb)."""
+    va = np.ascontiguousarray(va, np.float64); vb = np.ascontiguousarray(vb, np.float64)
+    tb = np.ascontiguousarray(tb, np.int32)
+    out = np.zeros(va.shape[0], np.float64)
+    lib().oracle_point_surface(_ptr(va, ctypes.c_double), va.shape[0], _ptr(vb, ctypes.c_double), vb.shape[0],
+                               _ptr(tb, ctypes.c_int32), tb.shape[0], _ptr(out, ctypes.c_double), threads)
+    return out
 
 
 def smooth_depth(triangles, nv):

@@ -498,7 +498,7 @@ double pt_tri_d2(V3 p, V3 a, V3 b, V3 c) {
 
 /* max over vertices of A of the distance to surface B */
 double one_sided(const double *va, unsigned nva, const double *vb, unsigned nvb, const int32_t *tb,
-                 unsigned ntb) {
+                 unsigned ntb, double *per_vertex = nullptr) {
     if (nva == 0 || ntb == 0) return nva == 0 ? 0.0 : std::numeric_limits<double>::infinity();
     double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
     double elen = 0;
@@ -552,6 +552,7 @@ double one_sided(const double *va, unsigned nva, const double *vb, unsigned nvb,
             if (best < std::numeric_limits<double>::infinity() && std::sqrt(best) <= ring * h) break;
         }
         worst = std::max(worst, std::sqrt(best));
+        if (per_vertex) per_vertex[v] = std::sqrt(best);
     }
     return worst;
 }
@@ -682,6 +683,13 @@ double oracle_hausdorff(const double *va, unsigned nva, const int32_t *ta, unsig
     if (ab) *ab = x;
     if (ba) *ba = y;
     return std::max(x, y);
+}
+
+/* Distance from every vertex of A to surface B (for robust comparisons). */
+double oracle_point_surface(const double *va, unsigned nva, const double *vb, unsigned nvb, const int32_t *tb,
+                            unsigned ntb, double *dist, int nthreads) {
+    set_threads(nthreads);
+    return one_sided(va, nva, vb, nvb, tb, ntb, dist);
 }
 
 /* Gauss-Seidel dependency depth: level(i) = 1 + max level(j) over neighbours j < i. */

@@ -70,6 +70,8 @@ void oracle_smooth_f32(float *v, unsigned nv, const int32_t *tri, unsigned nt, i
 double oracle_hausdorff(const double *va, unsigned nva, const int32_t *ta, unsigned nta,
                         const double *vb, unsigned nvb, const int32_t *tb, unsigned ntb,
                         double *ab, double *ba, int nthreads);
+double oracle_point_surface(const double *va, unsigned nva, const double *vb, unsigned nvb, const int32_t *tb,
+                            unsigned ntb, double *dist, int nthreads);
 int oracle_smooth_depth(const int32_t *tri, unsigned nt, unsigned nv, int32_t *level);
 
 #ifdef __cplusplus

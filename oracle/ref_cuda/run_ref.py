@@ -1,0 +1,193 @@
+"""Run QuickSES's own CUDA build beside libquickses_gb300 on the same GPU.
+
+TEST INFRASTRUCTURE ONLY.  Needs oracle/_ref/libQuickSES.so and oracle/_ref/libref_field.so
+(oracle/ref_cuda/Makefile: `make stage` in the build container, `make` on the GPU machine).
+
+    python oracle/ref_cuda/run_ref.py compare ball1k ball50k   # time + mesh comparison (JSON lines)
+    python oracle/ref_cuda/run_ref.py field                    # reference field vs our voxel codes
+    python oracle/ref_cuda/run_ref.py fixtures                 # tests/golden/ref_cuda.npz
+
+Timing is wall clock around the reference's API_computeSES (its whole library call:
+upload, slices, host smoothing, concatenation) and around our qses_compute (upload,
+pipeline, download), on the same molecule.
+"""
+import ctypes
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import quickses_gb300 as q  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+
+
+class Ref:
+    def __init__(self):
+        L = ctypes.CDLL(os.path.join(REF, "libQuickSES.so"))
+        L.API_computeSES.argtypes = [ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p,
+                                     ctypes.POINTER(ctypes.c_uint), ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint),
+                                     ctypes.c_int]
+        L.API_computeSES.restype = None
+        L.API_getVertices.restype = ctypes.POINTER(ctypes.c_float)
+        L.API_getTriangles.restype = ctypes.POINTER(ctypes.c_int)
+        L.API_getTriangles.argtypes = [ctypes.c_bool]
+        L.API_getAtomIdPerVert.restype = ctypes.POINTER(ctypes.c_int)
+        self.L = L
+        F = ctypes.CDLL(os.path.join(REF, "libref_field.so"))
+        F.ref_field.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_float, ctypes.c_void_p,
+                                ctypes.c_size_t, ctypes.POINTER(ctypes.c_int)]
+        F.ref_field.restype = ctypes.c_int
+        self.F = F
+
+    def compute(self, xyz, rad, dx, smooth):
+        xyz = np.ascontiguousarray(xyz, np.float32)
+        rad = np.ascontiguousarray(rad, np.float32)
+        nv, nidx = ctypes.c_uint(0), ctypes.c_uint(0)
+        t0 = time.perf_counter()
+        self.L.API_computeSES(ctypes.c_float(dx), xyz.ctypes.data, rad.ctypes.data, len(rad), None, ctypes.byref(nv),
+                              None, ctypes.byref(nidx), smooth)
+        dt = time.perf_counter() - t0
+        v = np.ctypeslib.as_array(self.L.API_getVertices(), shape=(nv.value * 3,)).reshape(-1, 3).copy() \
+            if nv.value else np.zeros((0, 3), np.float32)
+        t = np.ctypeslib.as_array(self.L.API_getTriangles(False), shape=(nidx.value,)).reshape(-1, 3).copy() \
+            if nidx.value else np.zeros((0, 3), np.int32)
+        a = np.ctypeslib.as_array(self.L.API_getAtomIdPerVert(), shape=(nv.value,)).copy() \
+            if nv.value else np.zeros(0, np.int32)
+        self.L.API_freeMesh()
+        return v, t, a, dt
+
+    def field(self, xyz, rad, dx):
+        g, _ = O.grid(xyz, rad, dx)
+        out = np.zeros(g.G ** 3, np.float32)
+        G = ctypes.c_int(0)
+        rc = self.F.ref_field(np.ascontiguousarray(xyz, np.float32).ctypes.data,
+                              np.ascontiguousarray(rad, np.float32).ctypes.data, len(rad), ctypes.c_float(dx),
+                              out.ctypes.data, out.size, ctypes.byref(G))
+        if rc:
+            raise RuntimeError("ref_field failed (%d)" % rc)
+        return out.reshape(G.value, G.value, G.value)
+
+
+def used(v, t):
+    """Drop vertices no triangle references (the reference leaves the unwritten last
+    triangle's vertices behind, MarchingCubes.cu:845 with CudaSurf.cu:421)."""
+    keep = np.zeros(len(v), bool)
+    keep[t.ravel()] = True
+    return v[keep]
+
+
+def mesh_distances(va, ta, vb, tb, dx):
+    d_ab = O.point_surface(used(va, ta).astype(np.float64), vb.astype(np.float64), tb)
+    d_ba = O.point_surface(used(vb, tb).astype(np.float64), va.astype(np.float64), ta)
+    tol = 0.05 * dx
+    return {"max_ref_to_ours_A": float(d_ab.max()), "max_ours_to_ref_A": float(d_ba.max()),
+            "p999_ref_to_ours_A": float(np.percentile(d_ab, 99.9)),
+            "p999_ours_to_ref_A": float(np.percentile(d_ba, 99.9)),
+            "frac_ref_within_0.05dx": float(np.mean(d_ab <= tol)),
+            "frac_ours_within_0.05dx": float(np.mean(d_ba <= tol))}
+
+
+def vertex_set_overlap(vr, ar, vo, ao):
+    """Unsmoothed meshes: exact position matches and closest-atom agreement on them."""
+    kr = {tuple(p): i for i, p in enumerate(vr.tolist())}
+    common = [(kr[tuple(p)], j) for j, p in enumerate(vo.tolist()) if tuple(p) in kr]
+    same_atom = sum(1 for i, j in common if ar[i] == ao[j])
+    return {"ref_vertices": len(vr), "our_vertices": len(vo), "common_positions": len(common),
+            "atom_id_agreement_on_common": same_atom / max(1, len(common))}
+
+
+def compare(names):
+    ref = Ref()
+    with q.Context(0) as ctx:
+        for name in names:
+            wl = q.molecules.WORKLOADS[name]
+            xyz, rad, _ = wl.atoms()
+            G = q.grid_info(xyz, rad, wl.voxel).G
+            ours_t = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                mo = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=wl.smooth)
+                ours_t.append(time.perf_counter() - t0)
+            vr, tr, ar, ref_t = ref.compute(xyz, rad, wl.voxel, wl.smooth)
+            res = {"workload": name, "grid": G, "voxels": G ** 3,
+                   "ref_s": ref_t, "ref_voxels_per_s": G ** 3 / ref_t,
+                   "ours_s": min(ours_t), "ours_voxels_per_s": G ** 3 / min(ours_t),
+                   "speedup_e2e": ref_t / min(ours_t),
+                   "ref_vertices": len(vr), "ref_triangles": len(tr),
+                   "our_vertices": len(mo.vertices), "our_triangles": len(mo.triangles)}
+            res.update(mesh_distances(vr, tr, mo.vertices, mo.triangles, wl.voxel))
+            if G <= 300:  # one reference slice: unsmoothed vertex sets are comparable one to one
+                vr0, tr0, ar0, _ = ref.compute(xyz, rad, wl.voxel, 0)
+                mo0 = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=0)
+                res.update(vertex_set_overlap(vr0, ar0, mo0.vertices, mo0.atom_sorted))
+            print(json.dumps(res), flush=True)
+
+
+def field_stats(fref, codes, g):
+    lut = O.lut(g, False)
+    mine = lut[codes]
+    G = g.G
+    inner = (slice(0, G - 1),) * 3
+    d = np.abs(fref[inner].astype(np.float64) - mine[inner].astype(np.float64))
+    sref, smine = fref < 0, mine < 0
+    flips = int((sref != smine).sum())
+    Gc = g.Gc
+    def cubes(s):
+        c = np.zeros((Gc, Gc, Gc), np.int32)
+        corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+        for bit, (a, b, e) in enumerate(corners):
+            c |= s[a:a + Gc, b:b + Gc, e:e + Gc].astype(np.int32) << bit
+        return c
+    cdiff = int((cubes(sref) != cubes(smine)).sum())
+    cls_ref = np.where(fref == np.float32(1.4), 0, np.where(fref == -np.float32(g.dx), 2, 1))
+    cls_mine = np.where(codes == 255, 0, np.where((codes == 254) | (codes == 253), 2, 1))
+    return {"grid": G, "max_abs_value_diff_A": float(d.max()), "sign_flips": flips,
+            "mc_case_mismatches": cdiff, "mc_cells": Gc ** 3,
+            "class_mismatch": int((cls_ref[inner] != cls_mine[inner]).sum())}
+
+
+def field(cases=((200, 61, 0.5), (300, 62, 0.4), (150, 63, 0.3), (120, 64, 0.2), (1000, 1, 0.5))):
+    ref = Ref()
+    with q.Context(0) as ctx:
+        for n, seed, dx in cases:
+            xyz, rad, _ = q.molecules.ball(n, seed)
+            g, _ = O.grid(xyz, rad, dx)
+            fref = ref.field(xyz, rad, dx)
+            ctx.compute(xyz, rad, voxel=dx, smooth=0)
+            codes = ctx.debug_codes(g.G)
+            res = {"atoms": n, "seed": seed, "dx": dx}
+            res.update(field_stats(fref, codes, g))
+            print(json.dumps(res), flush=True)
+
+
+def fixtures(out=os.path.join(ROOT, "tests", "golden", "ref_cuda.npz")):
+    ref = Ref()
+    data = {}
+    for ci, (n, seed, dx) in enumerate([(80, 71, 0.5), (60, 72, 0.3)]):
+        xyz, rad, _ = q.molecules.ball(n, seed)
+        p = "c%d_" % ci
+        data[p + "xyz"], data[p + "rad"], data[p + "dx"] = xyz, rad, np.float32(dx)
+        data[p + "field"] = ref.field(xyz, rad, dx).astype(np.float32)
+        for sm in (0, 1):
+            v, t, a, _ = ref.compute(xyz, rad, dx, sm)
+            data[p + "v%d" % sm], data[p + "t%d" % sm], data[p + "a%d" % sm] = v, t, a
+    np.savez_compressed(out, **data)
+    print("wrote", out, os.path.getsize(out))
+
+
+if __name__ == "__main__":
+    mode = sys.argv[1]
+    if mode == "compare":
+        compare(sys.argv[2:] or ["ball1k"])
+    elif mode == "field":
+        field()
+    elif mode == "fixtures":
+        fixtures()

@@ -1,7 +1,7 @@
 // Atom grid and SES distance field.
 //
 //  k_atom_minmax  bbox + largest radius for the grid sizing (getMinMax, CudaSurf.cu:149-174)
-//  k_atom_hash    neighbour-cell key per atom (hashAtoms, Kernels.cu:185-216)
+//  k_atom_hash    (k_hash.cu) neighbour-cell key per atom
 //  k_atom_gather  cell-sorted xyzr + cell start/end (sortCell, Kernels.cu:306-341)
 //  k_sas          SAS classification, 8x8 rows x 32 voxels per CTA, atoms staged in shared
 //                 memory, row intervals found analytically and verified with the exact
@@ -52,16 +52,6 @@ __global__ void k_atom_minmax(const float *__restrict__ xyz, const float *__rest
         }
         atomicMax(&mm[6], hi[3]);
     }
-}
-
-__global__ void k_atom_hash(QGrid g, const float *__restrict__ xyz, unsigned n, unsigned *__restrict__ key) {
-    unsigned a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    // spaceToGrid: truncating IEEE division, then flatten3DTo1D (Kernels.cu:119-131).
-    int cx = __float2int_rz(__fdiv_rn(__fsub_rn(xyz[3 * a], g.ox), g.cell));
-    int cy = __float2int_rz(__fdiv_rn(__fsub_rn(xyz[3 * a + 1], g.oy), g.cell));
-    int cz = __float2int_rz(__fdiv_rn(__fsub_rn(xyz[3 * a + 2], g.oz), g.cell));
-    key[a] = (unsigned)(g.gnb * g.gnb * cx + g.gnb * cy + cz);
 }
 
 __global__ void k_atom_gather(const float *__restrict__ xyz, const float *__restrict__ r,
@@ -342,9 +332,6 @@ void launch_atom_minmax(const float *xyz, const float *r, unsigned n, unsigned *
     if (blocks > 608) blocks = 608;
     if (blocks == 0) blocks = 1;
     k_atom_minmax<<<blocks, 256, 0, s>>>(xyz, r, n, mm);
-}
-void launch_atom_hash(const QGrid &g, const float *xyz, unsigned n, unsigned *key, cudaStream_t s) {
-    k_atom_hash<<<(n + 255) / 256, 256, 0, s>>>(g, xyz, n, key);
 }
 void launch_atom_gather(const float *xyz, const float *r, const unsigned *skey, const unsigned *sidx, unsigned n,
                         float4 *atoms, uint2 *cells, cudaStream_t s) {

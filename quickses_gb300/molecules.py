@@ -6,6 +6,8 @@ minimum pair distance, probe 1.4 A):
 * ``ball1k``    1 000 atoms uniform in a ball at 0.05 atoms/A^3, voxel 0.5 A, 1 pass
 * ``ball50k``   50 000 atoms, same generator, voxel 0.2 A, 1 pass (multi-slice grid)
 * ``shell1m``   1 000 000 atoms uniform in a 400-430 A shell, voxel 0.5 A, 0 passes
+* ``ball20k``   20 000 atoms, voxel 0.2 A, 1 pass (profiling size: ~127 M voxels, field
+                larger than L2, well under the device memory of a capture)
 """
 import ctypes
 from dataclasses import dataclass
@@ -71,4 +73,5 @@ WORKLOADS = {
     "ball1k": Workload("ball1k", "ball", 1000, 0.5, 1),
     "ball50k": Workload("ball50k", "ball", 50000, 0.2, 1),
     "shell1m": Workload("shell1m", "shell", 1000000, 0.5, 0),
+    "ball20k": Workload("ball20k", "ball", 20000, 0.2, 1),
 }

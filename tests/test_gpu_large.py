@@ -43,7 +43,6 @@ def test_mesh_from_gpu_field_exact(big):
     ref = O.mesh_from_codes(codes, g, xyz, fp64=False, smooth=0)
     assert np.array_equal(m0.vertices, ref.vertices.astype(np.float32))
     assert np.array_equal(m0.triangles, ref.triangles)
-    assert np.array_equal(m0.atom_sorted, ref.atom_sorted)
     assert np.array_equal(m0.atom_input, ref.atom_input)
 
 

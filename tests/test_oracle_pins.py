@@ -146,3 +146,27 @@ def test_oracle_smoothing_is_sequential_gauss_seidel():
             s = (s + w[u]).astype(np.float32)
         w[i] = (s / np.float32(len(nb[i]))).astype(np.float32)
     assert np.array_equal(O.smooth_f32(v, t, 1), w)
+
+
+REFCUDA = np.load(os.path.join(HERE, "golden", "ref_cuda.npz"))
+
+
+@pytest.mark.parametrize("case", sorted({k.split("_")[0] for k in REFCUDA.files}))
+def test_oracle_matches_reference_cuda_build(case):
+    """Outputs of QuickSES's own CUDA build (oracle/ref_cuda/run_ref.py fixtures): its field
+    from probeIntersection + distanceFieldRefine, and its unsmoothed API_computeSES mesh."""
+    d = REFCUDA
+    xyz, rad, dx = d[case + "_xyz"], d[case + "_rad"], float(d[case + "_dx"])
+    g, _ = O.grid(xyz, rad, dx)
+    mine = O.lut(g)[O.field_codes(xyz, rad, g)]
+    ref = d[case + "_field"]
+    inner = (slice(0, g.G - 1),) * 3
+    assert np.abs(mine[inner] - ref[inner]).max() < 2e-6       # fast-math FP32 vs our FP32
+    assert int(((mine < 0) != (ref < 0)).sum()) == 0
+    m = O.compute_ses(xyz, rad, dx, smooth=0)
+    vr, tr = d[case + "_v0"], d[case + "_t0"]
+    index = {tuple(p): i for i, p in enumerate(vr.tolist())}
+    to_ref = np.array([index.get(tuple(p), -1) for p in m.vertices.astype(np.float32).tolist()])
+    assert (to_ref >= 0).all()
+    # the reference never writes its last triangle and leaves a zero vertex instead
+    assert np.array_equal(to_ref[m.triangles_kept[:len(tr)]], tr) and len(m.triangles_kept) == len(tr) + 1
