@@ -88,6 +88,24 @@ def dist_env():
     return world, rank, local
 
 
+def reduce_max(values, world, device=None):
+    """Element-wise max of per-rank floats over all ranks (identity when world == 1).
+    The timed region's duration is the slowest rank's."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu().tolist()]
+
+
+def aggregate(world, units_per_rank, ms_max, e2e_ms_max):
+    """Whole-job throughput of N replicas: every rank processes the same units per step,
+    so the job rate is world * units / (slowest rank's time)."""
+    return world * units_per_rank / (ms_max * 1e-3), world * units_per_rank / (e2e_ms_max * 1e-3)
+
+
 def algorithmic_bytes(stage, g, n_atoms, T, nv, NE, passes):
     """Compulsory HBM bytes of one launch of each stage (roofline)."""
     G3 = float(g.G) ** 3
@@ -164,11 +182,6 @@ def run_gpu(args):
             torch.cuda.synchronize()
             t_wall = time.perf_counter() - t_wall0
         ms = float(np.mean(times))
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-            dist.barrier()
     nv, nt = dm.n_vertices, dm.n_triangles
 
     # e2e through the C-ABI with host buffers (upload, pipeline, download to pinned host)
@@ -190,7 +203,10 @@ def run_gpu(args):
         lib.qses_mesh_release(ctypes.byref(mesh))
         if it >= args.warmup:
             e2e_times.append(dt)
-    e2e_s = float(np.mean(e2e_times))
+    ms, e2e_ms = reduce_max([ms, 1e3 * float(np.mean(e2e_times))], world, device="cuda")
+    if world > 1:
+        dist.barrier()
+    value, e2e_value = aggregate(world, voxels, ms, e2e_ms)
 
     # roofline of the dominant stage
     peak, peak_kind = peaks()
@@ -201,7 +217,7 @@ def run_gpu(args):
     achieved = nbytes / (dom[1] * 1e-3) / 1e9
     result = {
         "metric": "SES grid voxels/s per molecule",
-        "value": world * voxels / (ms * 1e-3),
+        "value": value,
         "unit": "voxels/s",
         "n_gpus": world,
         "steps": args.steps,
@@ -217,7 +233,7 @@ def run_gpu(args):
                    "grid_dim": gi.G, "voxels": voxels, "atoms": n, "mesh_vertices": nv, "mesh_triangles": nt,
                    "l2": "flushed between timed steps (256 MB write outside the event pair)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": world * voxels / e2e_s, "unit": "voxels/s", "ms_per_step": e2e_s * 1e3,
+        "e2e": {"value": e2e_value, "unit": "voxels/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "qses_compute (C-ABI, pageable host atoms in, pinned host mesh out)"},
         "roofline": {"kernel": dom[0], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

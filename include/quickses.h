@@ -169,6 +169,24 @@ QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int ma
 QSES_API int qses_field_codes_noalloc(const float *d_xyz, const float *d_radii, unsigned n, float voxel,
                                       uint8_t *d_codes, size_t codes_bytes, void *cuda_stream);
 
+/* ---------------------------------------------------------- file front-end (CLI) */
+
+/* PDB ATOM records -> atom centres (3n floats) and radii (n floats), malloc'd; free both
+ * with qses_free.  Replaces the QuickSES executable's reading path: parsePDB
+ * (cpdb/cpdb.cpp:35-158) plus the per-atom radius lookup (CudaSurf.cu:942-964,
+ * CudaSurf.h:64-73): ATOM records only, stop at the first line starting with END, altLoc
+ * 'A' or ' ' only, hydrogens kept, radius from the first byte of the element field.
+ * Returns QSES_ERR_INVALID_ARG when the file cannot be opened (the reference exits(2)). */
+QSES_API int qses_read_pdb(const char *path, float **xyz, float **radii, unsigned *n);
+QSES_API void qses_free(void *p);
+/* Writes an OBJ file byte-identical to QuickSES's writeToObj (CudaSurf.cu:329-371) for one
+ * mesh: "v %.3f %.3f %.3f" lines, a blank line, "f b a c" lines (1-based, first two corners
+ * swapped).  threads <= 0 picks the host's thread count. */
+QSES_API int qses_write_obj(const char *path, const qses_float3 *vertices, unsigned nv, const int *triangles,
+                            unsigned nt, int threads);
+/* "%.3f" of one float, as qses_write_obj formats it; returns the length or -1. */
+QSES_API int qses_format_fixed3(float v, char *out, int cap);
+
 /* --------------------------------------------------- inspection (tests, tooling) */
 
 typedef struct {

@@ -59,6 +59,25 @@ def build_ref(ref=None):
     return out
 
 
+def build_ref_pdb(ref=None):
+    """The reference's PDB parser (cpdb/cpdb.cpp) plus a walk shim, into
+    oracle/_ref/libqses_ref_pdb.so.  None when the checkout is absent."""
+    ref = ref or os.environ.get("QSES_REFERENCE", REF_DEFAULT)
+    if not os.path.isdir(ref):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libqses_ref_pdb.so")
+    shim = os.path.join(HERE, "ref", "ref_pdb_shim.cpp")
+    src = os.path.join(ref, "cpdb", "cpdb.cpp")
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in (shim, src)):
+        return out
+    _run(["g++", "-O2", "-fPIC", "-shared", "-w", "-I", os.path.join(ref, "cpdb"), "-I", "/usr/local/cuda/include",
+          "-o", out, shim, src])
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_ref())
+    print(build_ref_pdb())

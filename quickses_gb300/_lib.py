@@ -83,6 +83,11 @@ SIGNATURES = {
     "qses_synth_shell": (ctypes.c_int, [ctypes.c_uint, ctypes.c_uint64, ctypes.c_float, ctypes.c_float,
                                         ctypes.c_float, _FP, _FP, ctypes.POINTER(ctypes.c_ubyte)]),
     "qses_synth_jitter": (ctypes.c_int, [_FP, ctypes.c_uint, ctypes.c_float, ctypes.c_uint64, _FP]),
+    "qses_read_pdb": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_FP), ctypes.POINTER(_FP),
+                                     ctypes.POINTER(ctypes.c_uint)]),
+    "qses_free": (None, [_VP]),
+    "qses_write_obj": (ctypes.c_int, [ctypes.c_char_p, _VP, ctypes.c_uint, _VP, ctypes.c_uint, ctypes.c_int]),
+    "qses_format_fixed3": (ctypes.c_int, [ctypes.c_float, ctypes.c_char_p, ctypes.c_int]),
     "NTriangles": None,
     "NVertices": None,
     "globalTriangles": None,

@@ -212,3 +212,37 @@ class ReferenceAPI:
 
     def exported_counts(self):
         return (ctypes.c_int.in_dll(self._lib, "NVertices").value, ctypes.c_int.in_dll(self._lib, "NTriangles").value)
+
+
+def read_pdb(path):
+    """ATOM records of a PDB file -> (xyz (N, 3) float32, radii (N,) float32), as the
+    QuickSES executable reads them (cpdb/cpdb.cpp:35-158, CudaSurf.cu:942-964)."""
+    lib = L.lib()
+    px, pr, n = ctypes.POINTER(ctypes.c_float)(), ctypes.POINTER(ctypes.c_float)(), ctypes.c_uint(0)
+    rc = lib.qses_read_pdb(str(path).encode(), ctypes.byref(px), ctypes.byref(pr), ctypes.byref(n))
+    if rc != L.QSES_OK:
+        raise QSESError(rc, "qses_read_pdb(%s): %s" % (path, L.status_string(rc)))
+    try:
+        k = n.value
+        xyz = np.ctypeslib.as_array(px, shape=(3 * k,)).reshape(k, 3).copy() if k else np.zeros((0, 3), np.float32)
+        rad = np.ctypeslib.as_array(pr, shape=(k,)).copy() if k else np.zeros(0, np.float32)
+    finally:
+        lib.qses_free(ctypes.cast(px, ctypes.c_void_p))
+        lib.qses_free(ctypes.cast(pr, ctypes.c_void_p))
+    return xyz, rad
+
+
+def write_obj(path, vertices, triangles, threads=0):
+    """OBJ text exactly as QuickSES's writeToObj writes one mesh (CudaSurf.cu:329-371)."""
+    v = _f32(vertices, 3)
+    t = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+    rc = L.lib().qses_write_obj(str(path).encode(), v.ctypes.data_as(ctypes.c_void_p), v.shape[0],
+                                t.ctypes.data_as(ctypes.c_void_p), t.shape[0], int(threads))
+    if rc != L.QSES_OK:
+        raise QSESError(rc, "qses_write_obj(%s): %s" % (path, L.status_string(rc)))
+
+
+def format_fixed3(x):
+    buf = ctypes.create_string_buffer(64)
+    k = L.lib().qses_format_fixed3(ctypes.c_float(x), buf, 64)
+    return buf.value[:k].decode()

@@ -7,7 +7,10 @@
 #include <cstring>
 #include <mutex>
 #include <algorithm>
+#include <cstdint>
 #include <new>
+#include <utility>
+#include <vector>
 
 #include "kernels.h"
 #include "qses_context.h"
@@ -17,10 +20,86 @@ using qses::DeviceMesh;
 namespace {
 
 // Host result buffers are pinned so the device-to-host copies run at full link speed.
+// Pinning is expensive (milliseconds for a 150 MB mesh), so released blocks go back to a
+// process-wide pool and are reused by later meshes of up to the same size.
 struct HostMesh {
     void *block = nullptr;
     size_t bytes = 0;
 };
+
+class PinnedPool {
+  public:
+    // Returns a block of at least `bytes` (rounded up to a size class), or nullptr.
+    void *take(size_t bytes, size_t *got) {
+        const size_t want = size_class(bytes);
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            // smallest cached block that fits and wastes at most a factor 2
+            size_t best = SIZE_MAX, bi = 0;
+            for (size_t i = 0; i < free_.size(); i++)
+                if (free_[i].second >= want && free_[i].second <= 2 * want && free_[i].second < best) {
+                    best = free_[i].second;
+                    bi = i;
+                }
+            if (best != SIZE_MAX) {
+                void *p = free_[bi].first;
+                *got = best;
+                cached_ -= best;
+                free_.erase(free_.begin() + (long)bi);
+                return p;
+            }
+        }
+        void *p = nullptr;
+        if (cudaMallocHost(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            trim(0);  // give cached blocks back and retry once
+            if (cudaMallocHost(&p, want) != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;
+            }
+        }
+        *got = want;
+        return p;
+    }
+    void give(void *p, size_t bytes) {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            if (cached_ + bytes <= kCap) {
+                free_.emplace_back(p, bytes);
+                cached_ += bytes;
+                return;
+            }
+        }
+        cudaFreeHost(p);
+    }
+
+  private:
+    static constexpr size_t kCap = 4ull << 30;  // pinned bytes kept for reuse
+    // size classes: 64 KB granularity below 1 MB, then 1/8 steps of the next power of two
+    static size_t size_class(size_t b) {
+        if (b <= (1u << 20)) return (b + 65535) & ~(size_t)65535;
+        size_t p2 = 1ull << 20;
+        while (p2 < b) p2 <<= 1;
+        const size_t step = p2 / 16;
+        return (b + step - 1) / step * step;
+    }
+    void trim(size_t keep) {
+        std::lock_guard<std::mutex> lock(mu_);
+        while (cached_ > keep && !free_.empty()) {
+            cudaFreeHost(free_.back().first);
+            cached_ -= free_.back().second;
+            free_.pop_back();
+        }
+    }
+    std::mutex mu_;
+    std::vector<std::pair<void *, size_t>> free_;
+    size_t cached_ = 0;
+};
+
+PinnedPool &pinned_pool() {
+    static PinnedPool *pool = new PinnedPool();  // never destroyed: meshes may outlive statics
+    return *pool;
+}
 
 int fill_host_mesh(qses_context *ctx, qses_mesh *out) {
     const DeviceMesh &m = ctx->mesh;
@@ -29,12 +108,11 @@ int fill_host_mesh(qses_context *ctx, qses_mesh *out) {
     const size_t total = vb + tb + 2 * ab + 64;
     HostMesh *hm = new (std::nothrow) HostMesh();
     if (!hm) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "host mesh");
-    if (cudaMallocHost(&hm->block, total) != cudaSuccess) {
-        cudaGetLastError();
+    hm->block = pinned_pool().take(total, &hm->bytes);
+    if (!hm->block) {
         delete hm;
         return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned host mesh");
     }
-    hm->bytes = total;
     char *p = (char *)hm->block;
     out->vertices = (qses_float3 *)p;
     out->triangles = (int *)(p + vb);
@@ -202,7 +280,7 @@ QSES_API void qses_mesh_release(qses_mesh *m) {
     if (!m) return;
     HostMesh *hm = (HostMesh *)m->_owner;
     if (hm) {
-        if (hm->block) cudaFreeHost(hm->block);
+        if (hm->block) pinned_pool().give(hm->block, hm->bytes);
         delete hm;
     }
     memset(m, 0, sizeof(*m));

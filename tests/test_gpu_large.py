@@ -1,4 +1,5 @@
-"""Full-size checks on the 50 000-atom / 0.2 A workload (grid 664^3, ~3.5 M vertices).
+"""Full-size checks on the 50 000-atom / 0.2 A workload (grid 664^3, ~3.5 M vertices) and
+the 1 000 000-atom shell at 0.5 A (grid 1738^3).
 
 The oracle cannot afford the whole field at this size, so the checks are split:
 * field: oracle codes on x-slabs (with their refine halo) == GPU codes there
@@ -66,3 +67,47 @@ def test_mesh_properties(big):
     tk = m1k.triangles
     assert (tk[:, 0] != tk[:, 1]).all() and (tk[:, 1] != tk[:, 2]).all() and (tk[:, 0] != tk[:, 2]).all()
     assert len(tk) < len(t)  # dx = 0.2 produces degenerate triangles, which the API drops
+
+
+# ---- the 1 000 000-atom shell at 0.5 A (grid 1738^3, 5.2e9 voxels, no smoothing)
+
+SHELL = q.molecules.WORKLOADS["shell1m"]
+
+
+@pytest.fixture(scope="module")
+def shell():
+    xyz, rad, _ = SHELL.atoms()
+    g, _ = O.grid(xyz, rad, SHELL.voxel)
+    with q.Context(0) as c:
+        m = c.compute(xyz, rad, voxel=SHELL.voxel, smooth=0, keep_degenerate=True)
+        codes = c.debug_codes(g.G)
+    return xyz, rad, g, m, codes
+
+
+@pytest.mark.parametrize("x0", [0, 431, 869, 1300, 1734])
+def test_shell_field_slab_exact(shell, x0):
+    xyz, rad, g, _, codes = shell
+    x1 = min(x0 + 4, g.G)
+    assert np.array_equal(codes[x0:x1], O.field_codes(xyz, rad, g, fp64=False, x0=x0, x1=x1))
+
+
+def test_shell_mesh_from_gpu_field_exact(shell):
+    xyz, _, g, m, codes = shell
+    ref = O.mesh_from_codes(codes, g, xyz, fp64=False, smooth=0)
+    assert np.array_equal(m.vertices, ref.vertices.astype(np.float32))
+    assert np.array_equal(m.triangles, ref.triangles)
+    assert np.array_equal(m.atom_input, ref.atom_input)
+
+
+def test_shell_mesh_properties(shell):
+    _, _, g, m, _ = shell
+    v = m.vertices.astype(np.float64)
+    d = np.diff(v, axis=0)
+    lex = (d[:, 0] > 0) | ((d[:, 0] == 0) & ((d[:, 1] > 0) | ((d[:, 1] == 0) & (d[:, 2] > 0))))
+    assert lex.all()
+    t = m.triangles
+    assert t.min() >= 0 and t.max() < len(v)
+    assert np.bincount(t.ravel(), minlength=len(v)).min() > 0
+    # the shell has an outer and an inner (cavity) surface, both inside the grid
+    r = np.linalg.norm(v - v.mean(axis=0), axis=1)
+    assert r.min() < 400.0 < 430.0 < r.max()
