@@ -135,6 +135,29 @@ typedef struct {
 QSES_API int qses_compute_device(qses_context *ctx, const qses_params *p, const float *d_xyz,
                                  const float *d_radii, unsigned n, qses_device_mesh *out);
 
+/* ------------------------------------------------------------------ batch form */
+
+/* One SES request of a batch (no reference counterpart: QuickSES computes one molecule per
+ * API_computeSES call).  atoms/radii are host arrays of n entries. */
+typedef struct {
+    const qses_float3 *atoms;
+    const float *radii;
+    unsigned n;
+    float voxel;        /* SES voxel size in A */
+    int smooth_passes;  /* Laplacian passes */
+    int flags;          /* QSES_FLAG_* */
+} qses_request;
+
+/* Many molecules (or trajectory frames) of uneven size in one pass: every stage is one
+ * launch over all of them (persistent field kernels pulling (molecule, tile) items from a
+ * device work queue, one weld sort, one Gauss-Seidel dataflow), results copied into one
+ * pinned block.  out[i] is exactly what qses_compute returns for request i alone; release
+ * each with qses_mesh_release.  status[i] (optional) receives the request's status; a
+ * request outside the supported envelope fails alone.  Requests are grouped internally by
+ * smooth_passes and by weld-key width. */
+QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, unsigned count, qses_mesh *out,
+                                int *status);
+
 QSES_API const char *qses_status_string(int status);
 QSES_API const char *qses_last_error(qses_context *ctx);
 

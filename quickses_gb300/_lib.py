@@ -41,6 +41,11 @@ class DeviceMesh(ctypes.Structure):
                 ("d_atom_sorted", ctypes.c_void_p), ("d_atom_input", ctypes.c_void_p)]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("atoms", ctypes.c_void_p), ("radii", ctypes.c_void_p), ("n", ctypes.c_uint),
+                ("voxel", ctypes.c_float), ("smooth_passes", ctypes.c_int), ("flags", ctypes.c_int)]
+
+
 class GridInfo(ctypes.Structure):
     _fields_ = [("origin", ctypes.c_float * 3), ("cell", ctypes.c_float), ("dx", ctypes.c_float),
                 ("probe", ctypes.c_float), ("max_radius", ctypes.c_float), ("max_dist", ctypes.c_float),
@@ -66,6 +71,8 @@ SIGNATURES = {
     "qses_mesh_release": (None, [ctypes.POINTER(Mesh)]),
     "qses_compute_device": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _VP, ctypes.c_uint,
                                            ctypes.POINTER(DeviceMesh)]),
+    "qses_compute_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.POINTER(Mesh),
+                                          ctypes.POINTER(ctypes.c_int)]),
     "qses_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "qses_last_error": (ctypes.c_char_p, [_VP]),
     "qses_set_profiling": (ctypes.c_int, [_VP, ctypes.c_int]),

@@ -32,6 +32,20 @@ class Mesh:
     origin: tuple
 
 
+def _take(ptr, n, dt, shape):
+    if n == 0:
+        return np.zeros(shape, dt)
+    return np.ctypeslib.as_array(ptr, shape=(n * (shape[1] if len(shape) > 1 else 1),)).astype(
+        dt, copy=True).reshape(shape)
+
+
+def _host_mesh(m):
+    nv, nt = m.n_vertices, m.n_triangles
+    return Mesh(_take(m.vertices, nv, np.float32, (nv, 3)), _take(m.triangles, nt, np.int32, (nt, 3)),
+                _take(m.atom_sorted, nv, np.int32, (nv,)), _take(m.atom_input, nv, np.int32, (nv,)),
+                int(m.grid_dim), tuple(m.origin))
+
+
 def _f32(a, shape_last=None):
     a = np.ascontiguousarray(a, dtype=np.float32)
     if shape_last is not None and (a.ndim != 2 or a.shape[1] != shape_last):
@@ -97,19 +111,40 @@ class Context:
                                     ctypes.byref(m))
         self._check(rc, "qses_compute")
         try:
-            nv, nt = m.n_vertices, m.n_triangles
-
-            def take(ptr, n, dt, shape):
-                if n == 0:
-                    return np.zeros(shape, dt)
-                return np.ctypeslib.as_array(ptr, shape=(n * (shape[1] if len(shape) > 1 else 1),)).astype(
-                    dt, copy=True).reshape(shape)
-
-            out = Mesh(take(m.vertices, nv, np.float32, (nv, 3)), take(m.triangles, nt, np.int32, (nt, 3)),
-                       take(m.atom_sorted, nv, np.int32, (nv,)), take(m.atom_input, nv, np.int32, (nv,)),
-                       int(m.grid_dim), tuple(m.origin))
+            out = _host_mesh(m)
         finally:
             self._lib.qses_mesh_release(ctypes.byref(m))
+        return out
+
+    def compute_batch(self, requests):
+        """Batch form: `requests` is a list of dicts with keys xyz, radii and optionally
+        voxel (0.5), smooth (1), keep_degenerate (False).  Returns one entry per request:
+        a Mesh, or a QSESError for a request outside the supported envelope."""
+        arrays, reqs = [], (L.Request * max(1, len(requests)))()
+        for i, r in enumerate(requests):
+            xyz, rad = _f32(r["xyz"], 3), _f32(r["radii"])
+            if rad.shape != (xyz.shape[0],):
+                raise ValueError("radii must have shape (N,)")
+            arrays.append((xyz, rad))
+            reqs[i].atoms, reqs[i].radii, reqs[i].n = xyz.ctypes.data, rad.ctypes.data, xyz.shape[0]
+            reqs[i].voxel = float(r.get("voxel", 0.5))
+            reqs[i].smooth_passes = int(r.get("smooth", 1))
+            reqs[i].flags = L.QSES_FLAG_KEEP_DEGENERATE if r.get("keep_degenerate", False) else 0
+        n = len(requests)
+        meshes = (L.Mesh * max(1, n))()
+        status = (ctypes.c_int * max(1, n))()
+        rc = self._lib.qses_compute_batch(self._h, reqs, n, meshes, status)
+        out = []
+        try:
+            self._check(rc, "qses_compute_batch")
+            for i in range(n):
+                if status[i] != L.QSES_OK:
+                    out.append(QSESError(status[i], "request %d: %s" % (i, L.status_string(status[i]))))
+                else:
+                    out.append(_host_mesh(meshes[i]))
+        finally:
+            for i in range(n):
+                self._lib.qses_mesh_release(ctypes.byref(meshes[i]))
         return out
 
     def compute_device(self, d_xyz_ptr, d_radii_ptr, n, voxel=0.5, smooth=1, keep_degenerate=False):

@@ -7,12 +7,15 @@
 #include <cstring>
 #include <mutex>
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
+#include <map>
 #include <new>
 #include <utility>
 #include <vector>
 
 #include "kernels.h"
+#include "prims.h"
 #include "qses_context.h"
 
 using qses::DeviceMesh;
@@ -25,6 +28,7 @@ namespace {
 struct HostMesh {
     void *block = nullptr;
     size_t bytes = 0;
+    std::atomic<int> *refs = nullptr;  // shared block of a batch: the last release returns it
 };
 
 class PinnedPool {
@@ -226,6 +230,7 @@ QSES_API int qses_context_destroy(qses_context *ctx) {
     ctx->mesh_ws.release();
     if (ctx->small) cudaFree(ctx->small);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     for (auto &m : ctx->marks) cudaEventDestroy(m.second);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -280,10 +285,138 @@ QSES_API void qses_mesh_release(qses_mesh *m) {
     if (!m) return;
     HostMesh *hm = (HostMesh *)m->_owner;
     if (hm) {
-        if (hm->block) pinned_pool().give(hm->block, hm->bytes);
+        if (hm->refs) {
+            if (hm->refs->fetch_sub(1) == 1) {
+                pinned_pool().give(hm->block, hm->bytes);
+                delete hm->refs;
+            }
+        } else if (hm->block) {
+            pinned_pool().give(hm->block, hm->bytes);
+        }
         delete hm;
     }
     memset(m, 0, sizeof(*m));
+}
+
+}  // extern "C"
+
+namespace {
+
+// Host bounds + reference sizing of one request (the device path reads the same bounds
+// with k_atom_minmax: min/max/max-radius are exact either way).
+int size_request(const qses_request &r, QGrid &g) {
+    float mn[3] = {100000.0f, 100000.0f, 100000.0f}, mx[3] = {-100000.0f, -100000.0f, -100000.0f}, maxR = 0.0f;
+    for (unsigned a = 0; a < r.n; a++) {
+        const float c[3] = {r.atoms[a].x, r.atoms[a].y, r.atoms[a].z};
+        for (int q = 0; q < 3; q++) {
+            mn[q] = std::min(mn[q], c[q]);
+            mx[q] = std::max(mx[q], c[q]);
+        }
+        maxR = std::max(maxR, r.radii[a]);
+    }
+    return qses::grid_from_bounds(mn, mx, maxR, r.n, r.voxel, g, nullptr, nullptr);
+}
+
+// Copies one finished batch into one pinned block shared by its meshes.
+int fill_batch_meshes(qses_context *ctx, const std::vector<unsigned> &reqs, const std::vector<qses::BatchItem> &items,
+                      qses_mesh *out) {
+    const qses::BatchResult &R = ctx->batch;
+    const size_t vb = 12ull * R.nv, tb = 12ull * R.nkept, ab = 4ull * R.nv;
+    const size_t total = vb + tb + 2 * ab + 256;
+    size_t got = 0;
+    void *block = pinned_pool().take(total, &got);
+    if (!block) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned batch meshes");
+    char *p = (char *)block;
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    if (vb) e = cudaMemcpyAsync(p, R.vertices, vb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && tb) e = cudaMemcpyAsync(p + vb, R.triangles, tb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && ab) e = cudaMemcpyAsync(p + vb + tb, R.atom_sorted, ab, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && ab) e = cudaMemcpyAsync(p + vb + tb + ab, R.atom_input, ab, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        pinned_pool().give(block, got);
+        return ctx->fail(QSES_ERR_CUDA, "batch mesh download", e);
+    }
+    std::atomic<int> *refs = new std::atomic<int>((int)reqs.size());
+    for (size_t m = 0; m < reqs.size(); m++) {
+        qses_mesh &o = out[reqs[m]];
+        HostMesh *hm = new HostMesh();
+        hm->block = block;
+        hm->bytes = got;
+        hm->refs = refs;
+        const unsigned v0 = R.vtx_off[m], v1 = R.vtx_off[m + 1], t0 = R.kept_off[m], t1 = R.kept_off[m + 1];
+        o.n_vertices = v1 - v0;
+        o.n_triangles = t1 - t0;
+        o.vertices = (qses_float3 *)(p + 12ull * v0);
+        o.triangles = (int *)(p + vb + 12ull * t0);
+        o.atom_sorted = (int *)(p + vb + tb + 4ull * v0);
+        o.atom_input = (int *)(p + vb + tb + ab + 4ull * v0);
+        o.grid_dim = items[m].g.G;
+        o.origin[0] = items[m].g.ox; o.origin[1] = items[m].g.oy; o.origin[2] = items[m].g.oz;
+        o._owner = hm;
+    }
+    return QSES_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, unsigned count, qses_mesh *out,
+                                int *status) {
+    if (!ctx || (count && (!reqs || !out))) return QSES_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    std::vector<QGrid> grids(count);
+    std::map<int, std::vector<unsigned>> by_passes;
+    for (unsigned i = 0; i < count; i++) {
+        memset(&out[i], 0, sizeof(qses_mesh));
+        const qses_request &r = reqs[i];
+        int rc = QSES_OK;
+        if (!(r.voxel > 0.0f) || r.smooth_passes < 0 || r.smooth_passes > 1000 || (r.n > 0 && (!r.atoms || !r.radii)))
+            rc = QSES_ERR_INVALID_ARG;
+        else if (r.n > 1)
+            rc = size_request(r, grids[i]);
+        if (status) status[i] = rc;
+        if (rc == QSES_OK && r.n > 1) by_passes[r.smooth_passes].push_back(i);
+    }
+    for (auto &grp : by_passes) {
+        const std::vector<unsigned> &ids = grp.second;
+        size_t at = 0;
+        while (at < ids.size()) {
+            // Largest prefix whose molecule-tagged weld keys fit 64 bits.
+            size_t end = at;
+            int kb = 0;
+            while (end < ids.size()) {
+                const QGrid &g = grids[ids[end]];
+                const int k = qses::bits_for((unsigned long long)g.Rq * g.Rq * g.Rq - 1);
+                const int kb2 = std::max(kb, k);
+                if (end > at && kb2 + qses::bits_for(end - at) > 64) break;
+                kb = kb2;
+                end++;
+            }
+            std::vector<unsigned> chunk(ids.begin() + (long)at, ids.begin() + (long)end);
+            std::vector<qses::BatchItem> items(chunk.size());
+            for (size_t m = 0; m < chunk.size(); m++) {
+                const qses_request &r = reqs[chunk[m]];
+                items[m].xyz = (const float *)r.atoms;
+                items[m].r = r.radii;
+                items[m].n = r.n;
+                items[m].flags = (unsigned)r.flags;
+                items[m].g = grids[chunk[m]];
+            }
+            int rc = qses::run_batch(ctx, items.data(), (unsigned)items.size(), grp.first, kb);
+            if (rc == QSES_OK) rc = fill_batch_meshes(ctx, chunk, items, out);
+            if (rc != QSES_OK) {
+                for (unsigned i : chunk) {
+                    if (status) status[i] = rc;
+                }
+                if (rc == QSES_ERR_CUDA || rc == QSES_ERR_TIMEOUT || rc == QSES_ERR_INTERNAL) return rc;
+            }
+            at = end;
+        }
+    }
+    return QSES_OK;
 }
 
 QSES_API const char *qses_last_error(qses_context *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }

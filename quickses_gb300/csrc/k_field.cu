@@ -125,12 +125,13 @@ __device__ __forceinline__ void atom_thresholds(float r, const QGrid &g, float &
     tsas = __fmul_rn(rs, rs);
 }
 
-__global__ void __launch_bounds__(kSasNT) k_sas(QGrid g, const float4 *__restrict__ atoms,
-                                                const uint2 *__restrict__ cells, unsigned *__restrict__ inMask,
-                                                unsigned *__restrict__ outMask) {
+// One SAS tile: z-word w of the 8 x 8 rows starting at (i0, j0) = (8 ib, 8 jb).
+__device__ __forceinline__ void sas_tile(const QGrid &g, int w, int jb, int ib, const float4 *__restrict__ atoms,
+                                         const uint2 *__restrict__ cells, unsigned *__restrict__ inMask,
+                                         unsigned *__restrict__ outMask) {
     __shared__ float s_x[kSasCap], s_y[kSasCap], s_z[kSasCap], s_tin[kSasCap], s_ts[kSasCap];
     __shared__ int s_n, s_over;
-    const int w = blockIdx.x, j0 = blockIdx.y * kSasTY, i0 = blockIdx.z * kSasTX;
+    const int j0 = jb * kSasTY, i0 = ib * kSasTX;
     const int t = threadIdx.x, i = i0 + t / kSasTY, j = j0 + t % kSasTY, k0 = w * 32;
     const int G = g.G, last = G - 2;  // voxels with an index of G-1 are never computed (Kernels.cu:436-441)
     const unsigned valid = (k0 + 32 <= G) ? 0xffffffffu : ((1u << (G - k0)) - 1u);
@@ -214,18 +215,25 @@ __global__ void __launch_bounds__(kSasNT) k_sas(QGrid g, const float4 *__restric
     }
 }
 
+__global__ void __launch_bounds__(kSasNT) k_sas(QGrid g, const float4 *__restrict__ atoms,
+                                                const uint2 *__restrict__ cells, unsigned *__restrict__ inMask,
+                                                unsigned *__restrict__ outMask) {
+    sas_tile(g, blockIdx.x, blockIdx.y, blockIdx.z, atoms, cells, inMask, outMask);
+}
+
 // ------------------------------------------------------------------ refine
 
 constexpr int kEdtTX = 8, kEdtTY = 8, kEdtNT = 256, kEdtH = kEdtTX + 2 * QSES_RMAX;
 
-__global__ void __launch_bounds__(kEdtNT) k_edt(QGrid g, const unsigned *__restrict__ inMask,
-                                                const unsigned *__restrict__ outMask,
-                                                unsigned char *__restrict__ codes, unsigned *__restrict__ signMask) {
+// One refine tile: z-word w of the 8 x 8 rows starting at (8 ib, 8 jb), with an R halo.
+__device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, const unsigned *__restrict__ inMask,
+                                         const unsigned *__restrict__ outMask, unsigned char *__restrict__ codes,
+                                         unsigned *__restrict__ signMask) {
     __shared__ unsigned s_out[kEdtH * kEdtH][3];
     __shared__ unsigned char s_g[kEdtH * kEdtH][32];
     __shared__ unsigned char s_h[kEdtH][kEdtTY][32];
     __shared__ unsigned s_in[kEdtTX * kEdtTY], s_ot[kEdtTX * kEdtTY];
-    const int w = blockIdx.x, j0 = blockIdx.y * kEdtTY, i0 = blockIdx.z * kEdtTX;
+    const int j0 = jb * kEdtTY, i0 = ib * kEdtTX;
     const int R = g.R, G = g.G, W = g.W, t = threadIdx.x;
     const int HX = kEdtTX + 2 * R, HY = kEdtTY + 2 * R, k0 = w * 32;
     const unsigned valid = (k0 + 32 <= G) ? 0xffffffffu : ((1u << (G - k0)) - 1u);
@@ -325,6 +333,59 @@ __global__ void __launch_bounds__(kEdtNT) k_edt(QGrid g, const unsigned *__restr
     if (part == 0 && i < G && j < G) signMask[((size_t)i * G + j) * W + w] = sgn;
 }
 
+__global__ void __launch_bounds__(kEdtNT) k_edt(QGrid g, const unsigned *__restrict__ inMask,
+                                                const unsigned *__restrict__ outMask,
+                                                unsigned char *__restrict__ codes, unsigned *__restrict__ signMask) {
+    edt_tile(g, blockIdx.x, blockIdx.y, blockIdx.z, inMask, outMask, codes, signMask);
+}
+
+// ------------------------------------------------------------ batched field
+
+// Persistent CTAs take field tiles of every molecule of a batch from one work counter.
+// A tile is decoded within its molecule exactly as the single-molecule grid would index it.
+__device__ __forceinline__ bool next_tile(const QBatch &b, unsigned *counter, unsigned &m, int &w, int &jb, int &ib) {
+    __shared__ unsigned s_item, s_m;
+    __syncthreads();  // the previous tile's shared memory is no longer in use
+    if (threadIdx.x == 0) {
+        const unsigned it = atomicAdd(counter, 1u);
+        s_item = it;
+        s_m = it < __ldg(b.tile_off + b.n_mol) ? qses_find(b.tile_off, b.n_mol, it) : 0xffffffffu;
+    }
+    __syncthreads();
+    m = s_m;
+    if (m == 0xffffffffu) return false;
+    const QGrid &g = b.mols[m].g;
+    const unsigned loc = s_item - __ldg(b.tile_off + m), ny = (unsigned)(g.G + 7) / 8u;
+    w = (int)(loc % (unsigned)g.W);
+    jb = (int)((loc / (unsigned)g.W) % ny);
+    ib = (int)(loc / ((unsigned)g.W * ny));
+    return true;
+}
+
+__global__ void __launch_bounds__(kSasNT) k_sas_batch(QBatch b, const float4 *__restrict__ atoms,
+                                                      const uint2 *__restrict__ cells, unsigned *__restrict__ inMask,
+                                                      unsigned *__restrict__ outMask, unsigned *counter) {
+    unsigned m;
+    int w, jb, ib;
+    while (next_tile(b, counter, m, w, jb, ib)) {
+        const QMol mol = b.mols[m];
+        sas_tile(mol.g, w, jb, ib, atoms, cells + mol.cell_off, inMask + mol.mask_off, outMask + mol.mask_off);
+    }
+}
+
+__global__ void __launch_bounds__(kEdtNT) k_edt_batch(QBatch b, const unsigned *__restrict__ inMask,
+                                                      const unsigned *__restrict__ outMask,
+                                                      unsigned char *__restrict__ codes,
+                                                      unsigned *__restrict__ signMask, unsigned *counter) {
+    unsigned m;
+    int w, jb, ib;
+    while (next_tile(b, counter, m, w, jb, ib)) {
+        const QMol mol = b.mols[m];
+        edt_tile(mol.g, w, jb, ib, inMask + mol.mask_off, outMask + mol.mask_off, codes + mol.code_off,
+                 signMask + mol.mask_off);
+    }
+}
+
 // ------------------------------------------------------------ launchers
 
 void launch_atom_minmax(const float *xyz, const float *r, unsigned n, unsigned *mm, cudaStream_t s) {
@@ -346,6 +407,24 @@ void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask,
                 unsigned *signMask, cudaStream_t s) {
     dim3 grid(g.W, (g.G + kEdtTY - 1) / kEdtTY, (g.G + kEdtTX - 1) / kEdtTX);
     k_edt<<<grid, kEdtNT, 0, s>>>(g, inMask, outMask, codes, signMask);
+}
+static unsigned persistent_blocks(const void *fn, int threads, unsigned items) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
+    unsigned blocks = (unsigned)(sms * (per_sm > 0 ? per_sm : 1));
+    return items < blocks ? (items ? items : 1u) : blocks;
+}
+void launch_sas_batch(const QBatch &b, unsigned tiles, const float4 *atoms, const uint2 *cells, unsigned *inMask,
+                      unsigned *outMask, unsigned *counter, cudaStream_t s) {
+    k_sas_batch<<<persistent_blocks((const void *)k_sas_batch, kSasNT, tiles), kSasNT, 0, s>>>(
+        b, atoms, cells, inMask, outMask, counter);
+}
+void launch_edt_batch(const QBatch &b, unsigned tiles, const unsigned *inMask, const unsigned *outMask,
+                      unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s) {
+    k_edt_batch<<<persistent_blocks((const void *)k_edt_batch, kEdtNT, tiles), kEdtNT, 0, s>>>(
+        b, inMask, outMask, codes, signMask, counter);
 }
 
 }  // namespace qses

@@ -21,8 +21,24 @@ __global__ void k_atom_hash(QGrid g, const float *__restrict__ xyz, unsigned n, 
     key[a] = (unsigned)(g.gnb * g.gnb * cx + g.gnb * cy + cz);
 }
 
+// Batch form: the key of an atom of molecule m is offset by m's first cell, so one stable
+// sort orders every molecule's atoms exactly as its own sort would, molecule after molecule.
+__global__ void k_atom_hash_batch(QBatch b, const float *__restrict__ xyz, unsigned n, unsigned *__restrict__ key) {
+    unsigned a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const unsigned m = qses_find(b.atom_off, b.n_mol, a);
+    const QGrid g = b.mols[m].g;
+    const int cx = (int)((xyz[3 * a] - g.ox) / g.cell);
+    const int cy = (int)((xyz[3 * a + 1] - g.oy) / g.cell);
+    const int cz = (int)((xyz[3 * a + 2] - g.oz) / g.cell);
+    key[a] = b.mols[m].cell_off + (unsigned)(g.gnb * g.gnb * cx + g.gnb * cy + cz);
+}
+
 void launch_atom_hash(const QGrid &g, const float *xyz, unsigned n, unsigned *key, cudaStream_t s) {
     k_atom_hash<<<(n + 255) / 256, 256, 0, s>>>(g, xyz, n, key);
+}
+void launch_atom_hash_batch(const QBatch &b, const float *xyz, unsigned n, unsigned *key, cudaStream_t s) {
+    k_atom_hash_batch<<<(n + 255) / 256, 256, 0, s>>>(b, xyz, n, key);
 }
 
 }  // namespace qses

@@ -68,20 +68,16 @@ __device__ __forceinline__ unsigned sel4(int o, unsigned a, unsigned b, unsigned
     return o == 0 ? a : (o == 1 ? b : (o == 2 ? c : d));
 }
 
+// One warp, one owner row (i, j) of a molecule's grid.  Edge keys get `keyhi` added (the
+// molecule's slot above the local key bits in a batch, 0 for a single molecule).
 template <bool EMIT>
-__global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict__ sign,
-                                            const unsigned char *__restrict__ codes, const float *__restrict__ lut,
-                                            uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
-                                            unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey) {
-    __shared__ unsigned long long s_tab[256];
-    __shared__ float s_lut[256];
-    s_tab[threadIdx.x] = c_mc[threadIdx.x];
-    if (EMIT) s_lut[threadIdx.x] = lut[threadIdx.x];
-    __syncthreads();
+__device__ __forceinline__ void mc_row(const QGrid &g, long long row, const unsigned *__restrict__ sign,
+                                       const unsigned char *__restrict__ codes, const float *lut,
+                                       const unsigned long long *s_tab, uint2 *__restrict__ rowCount,
+                                       const uint2 *__restrict__ rowBase, unsigned *__restrict__ tri,
+                                       unsigned long long *__restrict__ vkey, unsigned long long keyhi) {
     const int lane = threadIdx.x & 31;
     const int Gc = g.Gc, E = Gc + 1;
-    const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (row >= (long long)E * E) return;
     const int i = (int)(row / E), j = (int)(row % E);
     const bool cellsRow = i < Gc && j < Gc;
     const int Wc = (Gc + 32) / 32;  // words holding voxels 0..Gc
@@ -162,9 +158,9 @@ __global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict_
             for (unsigned m = X00 | Y00 | Z00; m; m &= m - 1u) {
                 const unsigned b = __ffs(m) - 1;
                 const int k = kb + (int)b;
-                if ((X00 >> b) & 1u) vkey[slot++] = edge_key(g, codes, s_lut, i, j, k, 0);
-                if ((Y00 >> b) & 1u) vkey[slot++] = edge_key(g, codes, s_lut, i, j, k, 1);
-                if ((Z00 >> b) & 1u) vkey[slot++] = edge_key(g, codes, s_lut, i, j, k, 2);
+                if ((X00 >> b) & 1u) vkey[slot++] = keyhi + edge_key(g, codes, lut, i, j, k, 0);
+                if ((Y00 >> b) & 1u) vkey[slot++] = keyhi + edge_key(g, codes, lut, i, j, k, 1);
+                if ((Z00 >> b) & 1u) vkey[slot++] = keyhi + edge_key(g, codes, lut, i, j, k, 2);
             }
         }
         // Triangles in cell order, corners as pre-weld vertex slots.
@@ -207,6 +203,43 @@ __global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict_
     if (!EMIT && lane == 0) rowCount[row] = make_uint2(triCarry, ec0);
 }
 
+template <bool EMIT>
+__global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict__ sign,
+                                            const unsigned char *__restrict__ codes, const float *__restrict__ lut,
+                                            uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
+                                            unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey) {
+    __shared__ unsigned long long s_tab[256];
+    __shared__ float s_lut[256];
+    s_tab[threadIdx.x] = c_mc[threadIdx.x];
+    if (EMIT) s_lut[threadIdx.x] = lut[threadIdx.x];
+    __syncthreads();
+    const int E = g.Gc + 1;
+    const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= (long long)E * E) return;
+    mc_row<EMIT>(g, row, sign, codes, s_lut, s_tab, rowCount, rowBase, tri, vkey, 0ull);
+}
+
+// Batch form: one warp per owner row of any molecule; rows are numbered molecule after
+// molecule, so one scan over all rows gives every molecule's triangles and edge slots
+// contiguous ranges in molecule order.
+template <bool EMIT>
+__global__ void __launch_bounds__(256) k_mc_batch(QBatch b, const unsigned *__restrict__ sign,
+                                                  const unsigned char *__restrict__ codes, uint2 *__restrict__ rowCount,
+                                                  const uint2 *__restrict__ rowBase, unsigned *__restrict__ tri,
+                                                  unsigned long long *__restrict__ vkey) {
+    __shared__ unsigned long long s_tab[256];
+    s_tab[threadIdx.x] = c_mc[threadIdx.x];
+    __syncthreads();
+    const unsigned row = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= __ldg(b.row_off + b.n_mol)) return;
+    const unsigned m = qses_find(b.row_off, b.n_mol, row);
+    const QMol &mol = b.mols[m];
+    const QGrid g = mol.g;
+    const unsigned r0 = mol.row_off;
+    mc_row<EMIT>(g, (long long)(row - r0), sign + mol.mask_off, codes + mol.code_off, b.lut + 256ull * m, s_tab,
+                 rowCount + r0, rowBase + r0, tri, vkey, (unsigned long long)m << b.key_bits);
+}
+
 // ------------------------------------------------------------------ weld
 
 __global__ void k_weld_flags(const unsigned long long *__restrict__ skey, unsigned n, uint2 *__restrict__ flags) {
@@ -232,6 +265,43 @@ __global__ void k_weld_scatter(QGrid g, const unsigned long long *__restrict__ s
         vq[3ull * rank + 1] = __fmul_rn((float)my, QSES_WELD_TOL);
         vq[3ull * rank + 2] = __fmul_rn((float)mz, QSES_WELD_TOL);
     }
+}
+
+// Batch form: the key's high bits name the molecule whose grid decodes the low bits.
+__global__ void k_weld_scatter_batch(QBatch b, const unsigned long long *__restrict__ skey,
+                                     const unsigned *__restrict__ sval, const uint2 *__restrict__ excl, unsigned n,
+                                     unsigned *__restrict__ vmap, float *__restrict__ vq, unsigned *__restrict__ vmol) {
+    unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const bool first = (p == 0 || skey[p] != skey[p - 1]);
+    const unsigned rank = excl[p].x + (first ? 1u : 0u) - 1u;
+    vmap[sval[p]] = rank;
+    if (first) {
+        const unsigned m = (unsigned)(skey[p] >> b.key_bits);
+        const unsigned long long key = skey[p] & ((1ull << b.key_bits) - 1ull);
+        const QGrid &g = b.mols[m].g;
+        const unsigned long long R = (unsigned long long)g.Rq;
+        const long long mz = (long long)(key % R) + g.bz;
+        const long long my = (long long)((key / R) % R) + g.by;
+        const long long mx = (long long)(key / (R * R)) + g.bx;
+        vq[3ull * rank] = __fmul_rn((float)mx, QSES_WELD_TOL);
+        vq[3ull * rank + 1] = __fmul_rn((float)my, QSES_WELD_TOL);
+        vq[3ull * rank + 2] = __fmul_rn((float)mz, QSES_WELD_TOL);
+        vmol[rank] = m;
+    }
+}
+
+// out[m] = excl[at[m]] for at[m] < n, else the scan total: the first scanned element of
+// each molecule's range gives that molecule's offset in the compacted output.
+__global__ void k_gather_offsets(const uint2 *__restrict__ excl, const unsigned *__restrict__ at, unsigned n_mol,
+                                 unsigned n, const uint2 *__restrict__ total, unsigned *__restrict__ outx,
+                                 unsigned *__restrict__ outy) {
+    unsigned m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m > n_mol) return;
+    const unsigned a = at[m];
+    const uint2 v = a < n ? excl[a] : *total;
+    if (outx) outx[m] = v.x;
+    if (outy) outy[m] = v.y;
 }
 
 __global__ void k_remap(unsigned *__restrict__ tri, size_t n3, const unsigned *__restrict__ vmap) {
@@ -275,6 +345,45 @@ __global__ void k_closest(QGrid g, const float *__restrict__ vq, unsigned nv, co
     ainput[v] = best >= 0 ? (int)sorted_to_input[best] : -1;
 }
 
+// Batch form: molecule from the vertex, atom ids local to the molecule.
+__global__ void k_closest_batch(QBatch b, const float *__restrict__ vq, const unsigned *__restrict__ vmol,
+                                unsigned nv, const float4 *__restrict__ atoms, const uint2 *__restrict__ cells,
+                                const unsigned *__restrict__ sorted_to_input, int *__restrict__ asorted,
+                                int *__restrict__ ainput) {
+    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const QMol &mol = b.mols[vmol[v]];
+    const QGrid g = mol.g;
+    const uint2 *mcells = cells + mol.cell_off;
+    const float qx = vq[3ull * v], qy = vq[3ull * v + 1], qz = vq[3ull * v + 2];
+    const int cx = __float2int_rz(__fdiv_rn(__fsub_rn(qx, g.ox), g.cell));
+    const int cy = __float2int_rz(__fdiv_rn(__fsub_rn(qy, g.oy), g.cell));
+    const int cz = __float2int_rz(__fdiv_rn(__fsub_rn(qz, g.oz), g.cell));
+    int best = -1;
+    float bestd = FLT_MAX;
+    for (int a = -1; a <= 1; a++) {
+        const int xx = min(max(cx + a, 0), g.gnb - 1);
+        for (int bb = -1; bb <= 1; bb++) {
+            const int yy = min(max(cy + bb, 0), g.gnb - 1);
+            for (int d = -1; d <= 1; d++) {
+                const int zz = min(max(cz + d, 0), g.gnb - 1);
+                const uint2 rg = mcells[((size_t)xx * g.gnb + yy) * g.gnb + zz];
+                for (unsigned s = rg.x; s < rg.y; s++) {
+                    const float4 at = atoms[s];
+                    const float ex = __fsub_rn(at.x, qx), ey = __fsub_rn(at.y, qy), ez = __fsub_rn(at.z, qz);
+                    const float d2 = __fmaf_rn(ez, ez, __fmaf_rn(ey, ey, __fmul_rn(ex, ex)));
+                    if (d2 < bestd) {
+                        bestd = d2;
+                        best = (int)s;
+                    }
+                }
+            }
+        }
+    }
+    asorted[v] = best >= 0 ? best - (int)mol.atom_off : -1;
+    ainput[v] = best >= 0 ? (int)sorted_to_input[best] - (int)mol.atom_off : -1;
+}
+
 // ------------------------------------------------------ degenerate filter
 
 __global__ void k_tri_flags(const unsigned *__restrict__ tri, unsigned nt, uint2 *__restrict__ flags) {
@@ -292,6 +401,31 @@ __global__ void k_tri_compact(const unsigned *__restrict__ tri, unsigned nt, con
     if (a != b && b != c && a != c) {
         const size_t o = 3ull * excl[t].x;
         out[o] = a; out[o + 1] = b; out[o + 2] = c;
+    }
+}
+
+// Batch form: molecules flagged QSES_FLAG_KEEP_DEGENERATE keep every triangle; corners are
+// rewritten as molecule-local vertex ids.
+__global__ void k_tri_flags_batch(QBatch b, const unsigned *__restrict__ tri, unsigned nt, uint2 *__restrict__ flags) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const unsigned m = qses_find(b.tri_off, b.n_mol, t);
+    const unsigned a = tri[3ull * t], c1 = tri[3ull * t + 1], c2 = tri[3ull * t + 2];
+    const bool keep = (b.mols[m].flags & QSES_FLAG_KEEP_DEGENERATE) || (a != c1 && c1 != c2 && a != c2);
+    flags[t] = make_uint2(keep ? 1u : 0u, 0u);
+}
+
+__global__ void k_tri_compact_batch(QBatch b, const unsigned *__restrict__ tri, unsigned nt,
+                                    const uint2 *__restrict__ excl, unsigned *__restrict__ out) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const unsigned m = qses_find(b.tri_off, b.n_mol, t);
+    const unsigned a = tri[3ull * t], c1 = tri[3ull * t + 1], c2 = tri[3ull * t + 2];
+    const bool keep = (b.mols[m].flags & QSES_FLAG_KEEP_DEGENERATE) || (a != c1 && c1 != c2 && a != c2);
+    if (keep) {
+        const unsigned v0 = __ldg(b.vtx_off + m);
+        const size_t o = 3ull * excl[t].x;
+        out[o] = a - v0; out[o + 1] = c1 - v0; out[o + 2] = c2 - v0;
     }
 }
 
@@ -404,11 +538,12 @@ __device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
 
 // Per vertex: lower-id neighbour entries inside its slab (+1 if any lie in lower slabs),
 // and the count of entries in lower slabs.
-__global__ void k_gs_setup(const uint2 *__restrict__ start, const unsigned *__restrict__ nbr, unsigned nv,
-                           unsigned S, unsigned short *__restrict__ cnt_local, int *__restrict__ remote) {
-    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nv) return;
-    const unsigned lo = (v / S) * S;
+// Vertices [v0, v1) form the slabs; no neighbour of theirs lies outside that range.
+__global__ void k_gs_setup(const uint2 *__restrict__ start, const unsigned *__restrict__ nbr, unsigned v0,
+                           unsigned v1, unsigned S, unsigned short *__restrict__ cnt_local, int *__restrict__ remote) {
+    unsigned v = v0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= v1) return;
+    const unsigned lo = v0 + ((v - v0) / S) * S;
     unsigned loc = 0, rem = 0;
     for (unsigned e = start[v].x; e < start[v + 1].x; e++) {
         const unsigned u = nbr[e];
@@ -468,20 +603,20 @@ __device__ __forceinline__ void ring_push16(volatile unsigned short *ring, unsig
     ring[k] = (unsigned short)off;  // each vertex enters the ring once: no wrap-around
 }
 
-__global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned nv, unsigned S,
+__global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned S,
                                                   const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
                                                   const unsigned short *__restrict__ cnt_local, int *remote,
                                                   unsigned *inbox, unsigned *inbox_tail, int *err,
                                                   long long spin_cycles, unsigned long long *stats) {
     extern __shared__ unsigned s_dyn[];
     __shared__ unsigned s_head, s_tail, s_done, s_seen, s_stop;
-    const unsigned p = blockIdx.x, a = p * S;
+    const unsigned p = blockIdx.x, a = v0 + p * S;  // vertices [v0, nv) in slabs of S
     if (a >= nv) return;  // uniform per CTA
     const unsigned b = min(a + S, nv), len = b - a;
     unsigned *st = s_dyn;                                        // len + 1 CSR offsets of the slab
     unsigned *cnt = s_dyn + (S + 1);                             // (len + 1) / 2 words: packed counters
     volatile unsigned short *ring = (volatile unsigned short *)(cnt + (S + 1) / 2);  // slab offsets
-    unsigned *box = inbox + a;                                   // boundary arrivals from lower slabs
+    unsigned *box = inbox + (a - v0);                            // boundary arrivals from lower slabs
     if (threadIdx.x == 0) { s_head = 0; s_tail = 0; s_done = 0; s_seen = 0; s_stop = 0; }
     for (unsigned k = threadIdx.x; k <= len; k += kGsT) st[k] = start[a + k].x;
     for (unsigned k = threadIdx.x; k < len; k += kGsT) ring[k] = 0xffffu;
@@ -610,7 +745,7 @@ __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned nv, uns
                             ready = dec16(cnt, u - a) == 1u;
                         } else if (atom_sub_acq_rel(remote + u, 1) == 1) {
                             // last lower-slab dependency of u: hand u to its slab
-                            const unsigned qs = u / S;
+                            const unsigned qs = (u - v0) / S;
                             const unsigned k = atomicAdd(inbox_tail + qs, 1u);
                             if (k < S) st_release_u32(inbox + (size_t)qs * S + k, u);
                         }
@@ -659,6 +794,34 @@ void launch_mc_emit(const QGrid &g, const unsigned *sign, const unsigned char *c
     size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
     k_mc<true><<<nblk(rows, 8), 256, 0, s>>>(g, sign, codes, lut, nullptr, rowBase, tri, vkey);
 }
+void launch_mc_count_batch(const QBatch &b, unsigned rows, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
+    k_mc_batch<false><<<nblk(rows, 8), 256, 0, s>>>(b, sign, nullptr, rowCount, nullptr, nullptr, nullptr);
+}
+void launch_mc_emit_batch(const QBatch &b, unsigned rows, const unsigned *sign, const unsigned char *codes,
+                          const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s) {
+    k_mc_batch<true><<<nblk(rows, 8), 256, 0, s>>>(b, sign, codes, nullptr, rowBase, tri, vkey);
+}
+void launch_weld_scatter_batch(const QBatch &b, const unsigned long long *skey, const unsigned *sval,
+                               const uint2 *excl, unsigned n, unsigned *vmap, float *vq, unsigned *vmol,
+                               cudaStream_t s) {
+    k_weld_scatter_batch<<<nblk(n, 256), 256, 0, s>>>(b, skey, sval, excl, n, vmap, vq, vmol);
+}
+void launch_gather_offsets(const uint2 *excl, const unsigned *at, unsigned n_mol, unsigned n, const uint2 *total,
+                           unsigned *outx, unsigned *outy, cudaStream_t s) {
+    k_gather_offsets<<<nblk(n_mol + 1, 256), 256, 0, s>>>(excl, at, n_mol, n, total, outx, outy);
+}
+void launch_closest_batch(const QBatch &b, const float *vq, const unsigned *vmol, unsigned nv, const float4 *atoms,
+                          const uint2 *cells, const unsigned *sorted_to_input, int *asorted, int *ainput,
+                          cudaStream_t s) {
+    k_closest_batch<<<nblk(nv, 128), 128, 0, s>>>(b, vq, vmol, nv, atoms, cells, sorted_to_input, asorted, ainput);
+}
+void launch_tri_flags_batch(const QBatch &b, const unsigned *tri, unsigned nt, uint2 *flags, cudaStream_t s) {
+    k_tri_flags_batch<<<nblk(nt, 256), 256, 0, s>>>(b, tri, nt, flags);
+}
+void launch_tri_compact_batch(const QBatch &b, const unsigned *tri, unsigned nt, const uint2 *excl, unsigned *out,
+                              cudaStream_t s) {
+    k_tri_compact_batch<<<nblk(nt, 256), 256, 0, s>>>(b, tri, nt, excl, out);
+}
 void launch_weld_flags(const unsigned long long *skey, unsigned n, uint2 *flags, cudaStream_t s) {
     k_weld_flags<<<nblk(n, 256), 256, 0, s>>>(skey, n, flags);
 }
@@ -699,9 +862,9 @@ cudaError_t launch_gs(float *pos, unsigned nv, const uint2 *start, const unsigne
     void *args[] = {&pos, &nv, (void *)&start, (void *)&nbr, &cnt, &queue, &qhead, &qtail, &err, &spin_cycles};
     return cudaLaunchCooperativeKernel((const void *)k_gs, dim3(blocks), dim3(256), args, 0, s);
 }
-void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned nv, unsigned S, unsigned short *cnt_local,
-                     int *remote, cudaStream_t s) {
-    k_gs_setup<<<nblk(nv, 256), 256, 0, s>>>(start, nbr, nv, S, cnt_local, remote);
+void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, unsigned S,
+                     unsigned short *cnt_local, int *remote, cudaStream_t s) {
+    k_gs_setup<<<nblk(v1 - v0, 256), 256, 0, s>>>(start, nbr, v0, v1, S, cnt_local, remote);
 }
 size_t gs_slab_smem(unsigned S) { return 4ull * (S + 1) + 4ull * ((S + 1) / 2) + 2ull * S + 16; }
 void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s) {
@@ -710,14 +873,13 @@ void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s) 
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s) {
     k_from_float4<<<nblk(nv, 256), 256, 0, s>>>(v4, nv, v3);
 }
-cudaError_t launch_gs_slab(float4 *pos, unsigned nv, unsigned S, int P, const uint2 *start, const unsigned *nbr,
-                           const unsigned short *cnt_local, int *remote, unsigned *glist, unsigned *inbox,
+cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, const uint2 *start,
+                           const unsigned *nbr, const unsigned short *cnt_local, int *remote, unsigned *inbox,
                            unsigned *inbox_tail, int *err, long long spin_cycles, unsigned long long *stats,
                            cudaStream_t s) {
-    (void)glist;
     size_t smem = gs_slab_smem(S);
     cudaFuncSetAttribute((const void *)k_gs_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
-    void *args[] = {&pos, &nv, &S, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
+    void *args[] = {&pos, &v0, &nv, &S, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
                     &inbox_tail, &err, &spin_cycles, &stats};
     return cudaLaunchCooperativeKernel((const void *)k_gs_flow, dim3(P), dim3(kGsT), args, smem, s);
 }

@@ -35,16 +35,38 @@ void launch_gs_seed(const int *lower, int *cnt, unsigned nv, unsigned *queue, un
 cudaError_t launch_gs(float *pos, unsigned nv, const uint2 *start, const unsigned *nbr, int *cnt, unsigned *queue,
                       unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles, int blocks, cudaStream_t s);
 int gs_max_blocks(int device);
-void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned nv, unsigned S, unsigned short *cnt_local,
-                     int *remote, cudaStream_t s);
+void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, unsigned S,
+                     unsigned short *cnt_local, int *remote, cudaStream_t s);
 size_t gs_slab_smem(unsigned S);
 void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s);
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s);
-cudaError_t launch_gs_slab(float4 *pos, unsigned nv, unsigned S, int P, const uint2 *start, const unsigned *nbr,
-                           const unsigned short *cnt_local, int *remote, unsigned *glist, unsigned *inbox,
+// One Gauss-Seidel pass over vertices [v0, nv) in P slabs of S (no neighbour outside).
+cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, const uint2 *start,
+                           const unsigned *nbr, const unsigned short *cnt_local, int *remote, unsigned *inbox,
                            unsigned *inbox_tail, int *err, long long spin_cycles, unsigned long long *stats,
                            cudaStream_t s);
 int gs_slab_max_blocks(int device, unsigned S);
-constexpr unsigned kGsSlabMaxVerts = 25000;  // 8 B of shared memory per vertex, 16-bit slab offsets
+constexpr unsigned kGsSlabMaxVerts = 25000;
+
+// ---- batch forms (QBatch: per-molecule grids and offsets in device memory)
+void launch_atom_hash_batch(const QBatch &b, const float *xyz, unsigned n, unsigned *key, cudaStream_t s);
+void launch_sas_batch(const QBatch &b, unsigned tiles, const float4 *atoms, const uint2 *cells, unsigned *inMask,
+                      unsigned *outMask, unsigned *counter, cudaStream_t s);
+void launch_edt_batch(const QBatch &b, unsigned tiles, const unsigned *inMask, const unsigned *outMask,
+                      unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s);
+void launch_mc_count_batch(const QBatch &b, unsigned rows, const unsigned *sign, uint2 *rowCount, cudaStream_t s);
+void launch_mc_emit_batch(const QBatch &b, unsigned rows, const unsigned *sign, const unsigned char *codes,
+                          const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s);
+void launch_weld_scatter_batch(const QBatch &b, const unsigned long long *skey, const unsigned *sval,
+                               const uint2 *excl, unsigned n, unsigned *vmap, float *vq, unsigned *vmol,
+                               cudaStream_t s);
+void launch_gather_offsets(const uint2 *excl, const unsigned *at, unsigned n_mol, unsigned n, const uint2 *total,
+                           unsigned *outx, unsigned *outy, cudaStream_t s);
+void launch_closest_batch(const QBatch &b, const float *vq, const unsigned *vmol, unsigned nv, const float4 *atoms,
+                          const uint2 *cells, const unsigned *sorted_to_input, int *asorted, int *ainput,
+                          cudaStream_t s);
+void launch_tri_flags_batch(const QBatch &b, const unsigned *tri, unsigned nt, uint2 *flags, cudaStream_t s);
+void launch_tri_compact_batch(const QBatch &b, const unsigned *tri, unsigned nt, const uint2 *excl, unsigned *out,
+                              cudaStream_t s);  // 8 B of shared memory per vertex, 16-bit slab offsets
 
 }  // namespace qses

@@ -346,13 +346,13 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
             launch_to_float4(vq, nv, pos4, s);
             ctx->launches++;
             for (int pass = 0; pass < p.smooth_passes; pass++) {
-                launch_gs_setup(deg, nbr, nv, S, (unsigned short *)cnt, lower, s);
+                launch_gs_setup(deg, nbr, 0, nv, S, (unsigned short *)cnt, lower, s);
                 ctx->launches++;
                 QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * P * S, s));
                 QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
                 unsigned long long *stats = (unsigned long long *)((char *)ctx->small + 256);
                 QCHK(cudaMemsetAsync(stats, 0, 64, s));
-                QCHK(launch_gs_slab(pos4, nv, S, P, deg, nbr, (unsigned short *)cnt, lower, queue, inbox, inbox_tail,
+                QCHK(launch_gs_slab(pos4, 0, nv, S, P, deg, nbr, (unsigned short *)cnt, lower, inbox, inbox_tail,
                                     d_err, 4000000000ll, stats, s));
                 ctx->diag[0] = P;
                 ctx->diag[1] = S;

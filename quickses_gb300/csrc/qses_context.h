@@ -34,6 +34,25 @@ int grid_from_bounds(const float mn[3], const float mx[3], float maxR, unsigned 
                      qses_grid_info *info, std::string *why);
 void fill_lut(const QGrid &g, float *lut);
 
+// One molecule of a batch call: host atoms and its grid, sized on the host.
+struct BatchItem {
+    const float *xyz = nullptr;  // 3n floats
+    const float *r = nullptr;    // n floats
+    unsigned n = 0;
+    unsigned flags = 0;
+    QGrid g;
+};
+
+// Device-resident result of the last batch (pointers into the context arenas) and the
+// per-molecule ranges of its concatenated arrays.
+struct BatchResult {
+    unsigned n_mol = 0, nv = 0, nkept = 0;
+    std::vector<unsigned> vtx_off, kept_off;  // n_mol + 1 entries
+    float *vertices = nullptr;
+    unsigned *triangles = nullptr;            // kept triangles, molecule-local vertex ids
+    int *atom_sorted = nullptr, *atom_input = nullptr;
+};
+
 }  // namespace qses
 
 struct qses_context {
@@ -48,6 +67,9 @@ struct qses_context {
     qses_grid_info info;
     bool have_grid = false;
     qses::DeviceMesh mesh;
+    qses::BatchResult batch;
+    void *h_stage = nullptr;          // pinned staging for batch uploads (grows)
+    size_t h_stage_cap = 0;
     std::string last_error;
     bool profiling = false;
     std::vector<std::pair<const char *, cudaEvent_t>> marks;
@@ -61,4 +83,7 @@ struct qses_context {
 
 namespace qses {
 int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n);
+// All items share `passes`; the weld keys of every item fit `key_bits` bits and
+// key_bits + bits(count - 1) <= 64.  Results in ctx->batch.
+int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int passes, int key_bits);
 }

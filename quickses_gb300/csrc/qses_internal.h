@@ -34,3 +34,41 @@ struct QGrid {
     long long bx, by, bz;  // weld key base (quantised origin - margin)
     long long Rq;          // weld key radix per axis
 };
+
+// One molecule of a batch: its grid and where its pieces sit in the batch's concatenated
+// device arrays.  Offsets are in elements of the array named.
+struct QMol {
+    QGrid g;
+    unsigned long long mask_off;  // first 32-bit word of the in/out/sign masks
+    unsigned long long code_off;  // first byte of the voxel codes
+    unsigned atom_off;            // first atom (input order and cell-sorted order)
+    unsigned cell_off;            // first neighbour cell of the cell table
+    unsigned row_off;             // first marching-cubes owner row
+    unsigned flags;               // QSES_FLAG_* of the request
+};
+
+// Device view of a batch.  The *_off arrays have n_mol + 1 entries (the last is the total)
+// and are searched to map a global item, atom, row, triangle or vertex to its molecule.
+struct QBatch {
+    const QMol *mols;
+    const unsigned *tile_off;  // field tiles (8 x 8 z-rows of 32 voxels) per molecule
+    const unsigned *atom_off;
+    const unsigned *row_off;
+    const unsigned *tri_off;   // pre-filter triangles (valid after the row scan)
+    const unsigned *vtx_off;   // welded vertices (valid after the weld)
+    const float *lut;          // 256 field values per molecule
+    unsigned n_mol;
+    int key_bits;              // bits of a molecule-local weld key; the molecule sits above
+};
+
+// Largest m with off[m] <= x, for off[0] = 0 <= x < off[n].
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned qses_find(const unsigned *off, unsigned n, unsigned x) {
+    unsigned lo = 0, hi = n;  // off[lo] <= x < off[hi]
+    while (hi - lo > 1) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= x) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+#endif
