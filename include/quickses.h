@@ -158,6 +158,57 @@ typedef struct {
 QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, unsigned count, qses_mesh *out,
                                 int *status);
 
+/* ------------------------------------------------------------------ autotuner */
+
+/* Picks the smoothing launch shape (threads per slab CTA, slab size aimed at) for meshes of
+ * this size by running the molecule once per candidate shape (`repeats` times each) and
+ * keeping the fastest; later calls of this process on meshes of the same size class (log2
+ * of the vertex count) use it.  The mesh is identical for every shape: the update order is
+ * fixed by the vertex ids.  No reference counterpart (QuickSES hard-codes its launches). */
+QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_float3 *atoms, const float *radii,
+                           unsigned n, int repeats, int *threads_out, unsigned *target_out, float *smooth_ms_out);
+/* Fixes the smoothing launch shape of ctx (threads 512 or 1024 per slab CTA, slab size
+ * aimed at >= 256 vertices); threads = 0 returns to the tuned/default shape. */
+QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target);
+/* The same for the batch form, timing whole qses_compute_batch calls on `reqs`. */
+QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, unsigned count, int repeats,
+                                 int *threads_out, unsigned *target_out, float *ms_out);
+
+/* ---------------------------------------------------------------- served form */
+
+/* A request loop with continuous batching (no reference counterpart).  `lanes` worker
+ * threads each own a context (stream + persistent workspace); a free lane takes every
+ * queued request that fits its share of memory_budget (FIFO, at most max_batch) and runs
+ * them as one qses_compute_batch, so requests that arrive while others run are batched as
+ * lanes free up and batches overlap on the device.  Results equal qses_compute's. */
+typedef struct qses_server qses_server;
+typedef struct {
+    int device;
+    int lanes;                         /* batches in flight (default 2) */
+    unsigned long long memory_budget;  /* device bytes for admitted work (default 120 GB) */
+    unsigned max_batch;                /* requests per batch (default 256) */
+} qses_server_config;
+typedef struct {
+    double queued_s;  /* submit -> start of its batch */
+    double run_s;     /* its batch's run, mesh download included */
+    double total_s;   /* submit -> result ready */
+} qses_ticket_info;
+QSES_API void qses_server_config_default(qses_server_config *c);
+QSES_API int qses_server_create(const qses_server_config *cfg, qses_server **out);
+/* Copies the request's atoms; returns QSES_ERR_UNSUPPORTED / QSES_ERR_OUT_OF_MEMORY at once
+ * for requests that can never run (grid envelope, estimated size above the budget). */
+QSES_API int qses_server_submit(qses_server *s, const qses_request *req, unsigned long long *ticket);
+/* Blocks until the ticket's mesh is ready (timeout_s < 0: forever; on QSES_ERR_TIMEOUT the
+ * ticket stays valid).  Returns the request's status; *out is then the caller's (release
+ * with qses_mesh_release) and the ticket is consumed. */
+QSES_API int qses_server_wait(qses_server *s, unsigned long long ticket, double timeout_s, qses_mesh *out,
+                              qses_ticket_info *info);
+/* [0] batches run, [1] requests served, [2] largest batch, [3] most lanes busy at once,
+ * [4] requests queued now.  Returns the number of values written. */
+QSES_API int qses_server_stats(qses_server *s, unsigned long long *out, int max);
+/* Finishes queued work, then frees everything (uncollected meshes included). */
+QSES_API int qses_server_destroy(qses_server *s);
+
 QSES_API const char *qses_status_string(int status);
 QSES_API const char *qses_last_error(qses_context *ctx);
 

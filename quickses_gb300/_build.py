@@ -25,7 +25,7 @@ GXX = ["g++", "-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contrac
 LIB_CU = ["k_prims.cu", "k_field.cu", "k_hash.cu", "k_mesh.cu", "pipeline.cu", "pipeline_batch.cu", "noalloc.cu"]
 # Per-file flags: the atom cell key uses the reference's own arithmetic (see k_hash.cu).
 EXTRA_FLAGS = {"k_hash.cu": ["-use_fast_math"]}
-LIB_CPP = ["api.cpp", "synth.cpp", "io.cpp"]
+LIB_CPP = ["api.cpp", "synth.cpp", "io.cpp", "server.cpp"]
 CLI_CPP = ["cli.cpp"]
 
 

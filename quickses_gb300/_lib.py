@@ -46,6 +46,15 @@ class Request(ctypes.Structure):
                 ("voxel", ctypes.c_float), ("smooth_passes", ctypes.c_int), ("flags", ctypes.c_int)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("lanes", ctypes.c_int), ("memory_budget", ctypes.c_ulonglong),
+                ("max_batch", ctypes.c_uint)]
+
+
+class TicketInfo(ctypes.Structure):
+    _fields_ = [("queued_s", ctypes.c_double), ("run_s", ctypes.c_double), ("total_s", ctypes.c_double)]
+
+
 class GridInfo(ctypes.Structure):
     _fields_ = [("origin", ctypes.c_float * 3), ("cell", ctypes.c_float), ("dx", ctypes.c_float),
                 ("probe", ctypes.c_float), ("max_radius", ctypes.c_float), ("max_dist", ctypes.c_float),
@@ -73,6 +82,18 @@ SIGNATURES = {
                                            ctypes.POINTER(DeviceMesh)]),
     "qses_compute_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.POINTER(Mesh),
                                           ctypes.POINTER(ctypes.c_int)]),
+    "qses_set_smoothing_shape": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint]),
+    "qses_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _FP, ctypes.c_uint, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint), _FP]),
+    "qses_autotune_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint), _FP]),
+    "qses_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
+    "qses_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_VP)]),
+    "qses_server_submit": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_ulonglong)]),
+    "qses_server_wait": (ctypes.c_int, [_VP, ctypes.c_ulonglong, ctypes.c_double, ctypes.POINTER(Mesh),
+                                        ctypes.POINTER(TicketInfo)]),
+    "qses_server_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
+    "qses_server_destroy": (ctypes.c_int, [_VP]),
     "qses_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "qses_last_error": (ctypes.c_char_p, [_VP]),
     "qses_set_profiling": (ctypes.c_int, [_VP, ctypes.c_int]),

@@ -46,6 +46,21 @@ def _host_mesh(m):
                 int(m.grid_dim), tuple(m.origin))
 
 
+def _requests(requests):
+    """ctypes qses_request array for a list of request dicts (arrays kept alive by the caller)."""
+    arrays, reqs = [], (L.Request * max(1, len(requests)))()
+    for i, r in enumerate(requests):
+        xyz, rad = _f32(r["xyz"], 3), _f32(r["radii"])
+        if rad.shape != (xyz.shape[0],):
+            raise ValueError("radii must have shape (N,)")
+        arrays.append((xyz, rad))
+        reqs[i].atoms, reqs[i].radii, reqs[i].n = xyz.ctypes.data, rad.ctypes.data, xyz.shape[0]
+        reqs[i].voxel = float(r.get("voxel", 0.5))
+        reqs[i].smooth_passes = int(r.get("smooth", 1))
+        reqs[i].flags = L.QSES_FLAG_KEEP_DEGENERATE if r.get("keep_degenerate", False) else 0
+    return arrays, reqs
+
+
 def _f32(a, shape_last=None):
     a = np.ascontiguousarray(a, dtype=np.float32)
     if shape_last is not None and (a.ndim != 2 or a.shape[1] != shape_last):
@@ -120,16 +135,7 @@ class Context:
         """Batch form: `requests` is a list of dicts with keys xyz, radii and optionally
         voxel (0.5), smooth (1), keep_degenerate (False).  Returns one entry per request:
         a Mesh, or a QSESError for a request outside the supported envelope."""
-        arrays, reqs = [], (L.Request * max(1, len(requests)))()
-        for i, r in enumerate(requests):
-            xyz, rad = _f32(r["xyz"], 3), _f32(r["radii"])
-            if rad.shape != (xyz.shape[0],):
-                raise ValueError("radii must have shape (N,)")
-            arrays.append((xyz, rad))
-            reqs[i].atoms, reqs[i].radii, reqs[i].n = xyz.ctypes.data, rad.ctypes.data, xyz.shape[0]
-            reqs[i].voxel = float(r.get("voxel", 0.5))
-            reqs[i].smooth_passes = int(r.get("smooth", 1))
-            reqs[i].flags = L.QSES_FLAG_KEEP_DEGENERATE if r.get("keep_degenerate", False) else 0
+        arrays, reqs = _requests(requests)
         n = len(requests)
         meshes = (L.Mesh * max(1, n))()
         status = (ctypes.c_int * max(1, n))()
@@ -146,6 +152,30 @@ class Context:
             for i in range(n):
                 self._lib.qses_mesh_release(ctypes.byref(meshes[i]))
         return out
+
+    def set_smoothing_shape(self, threads=0, target=16384):
+        """Fix the smoothing launch shape (threads 512/1024, slab target); 0 = tuned/default."""
+        self._check(self._lib.qses_set_smoothing_shape(self._h, int(threads), int(target)), "qses_set_smoothing_shape")
+
+    def autotune(self, xyz, radii, voxel=0.5, smooth=1, repeats=1):
+        """Times every smoothing launch shape on this molecule and keeps the fastest for its
+        mesh size class; returns (threads, slab target, smoothing ms)."""
+        xyz, radii = _f32(xyz, 3), _f32(radii)
+        th, tg, ms = ctypes.c_int(0), ctypes.c_uint(0), ctypes.c_float(0)
+        rc = self._lib.qses_autotune(self._h, ctypes.byref(self._params(voxel, smooth, False, 300)),
+                                     xyz.ctypes.data_as(ctypes.c_void_p),
+                                     radii.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), xyz.shape[0], int(repeats),
+                                     ctypes.byref(th), ctypes.byref(tg), ctypes.byref(ms))
+        self._check(rc, "qses_autotune")
+        return th.value, tg.value, ms.value
+
+    def autotune_batch(self, requests, repeats=1):
+        arrays, reqs = _requests(requests)
+        th, tg, ms = ctypes.c_int(0), ctypes.c_uint(0), ctypes.c_float(0)
+        rc = self._lib.qses_autotune_batch(self._h, reqs, len(requests), int(repeats), ctypes.byref(th),
+                                           ctypes.byref(tg), ctypes.byref(ms))
+        self._check(rc, "qses_autotune_batch")
+        return th.value, tg.value, ms.value
 
     def compute_device(self, d_xyz_ptr, d_radii_ptr, n, voxel=0.5, smooth=1, keep_degenerate=False):
         """Device-resident form (pointers to device float arrays); returns counts and the
@@ -281,3 +311,65 @@ def format_fixed3(x):
     buf = ctypes.create_string_buffer(64)
     k = L.lib().qses_format_fixed3(ctypes.c_float(x), buf, 64)
     return buf.value[:k].decode()
+
+
+class Server:
+    """Served form (qses_server_*): continuous batching over `lanes` streams under a
+    device-memory budget.  submit() copies the atoms and returns a ticket; wait() returns
+    (Mesh, timing) for it, or raises QSESError with the request's status."""
+
+    def __init__(self, device=0, lanes=2, memory_budget=120 << 30, max_batch=256):
+        self._lib = L.lib()
+        cfg = L.ServerConfig()
+        self._lib.qses_server_config_default(ctypes.byref(cfg))
+        cfg.device, cfg.lanes, cfg.memory_budget, cfg.max_batch = device, lanes, memory_budget, max_batch
+        h = ctypes.c_void_p()
+        rc = self._lib.qses_server_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != L.QSES_OK:
+            raise QSESError(rc, "qses_server_create: " + L.status_string(rc))
+        self._h = h
+
+    def submit(self, xyz, radii, voxel=0.5, smooth=1, keep_degenerate=False):
+        xyz, radii = _f32(xyz, 3), _f32(radii)
+        r = L.Request(xyz.ctypes.data, radii.ctypes.data, xyz.shape[0], float(voxel), int(smooth),
+                      L.QSES_FLAG_KEEP_DEGENERATE if keep_degenerate else 0)
+        t = ctypes.c_ulonglong(0)
+        rc = self._lib.qses_server_submit(self._h, ctypes.byref(r), ctypes.byref(t))
+        if rc != L.QSES_OK:
+            raise QSESError(rc, "qses_server_submit: " + L.status_string(rc))
+        return t.value
+
+    def wait(self, ticket, timeout=-1.0):
+        m, info = L.Mesh(), L.TicketInfo()
+        rc = self._lib.qses_server_wait(self._h, ctypes.c_ulonglong(ticket), float(timeout), ctypes.byref(m),
+                                        ctypes.byref(info))
+        try:
+            if rc != L.QSES_OK:
+                raise QSESError(rc, "request %d: %s" % (ticket, L.status_string(rc)))
+            mesh = _host_mesh(m)
+        finally:
+            self._lib.qses_mesh_release(ctypes.byref(m))
+        return mesh, {"queued_s": info.queued_s, "run_s": info.run_s, "total_s": info.total_s}
+
+    def stats(self):
+        out = (ctypes.c_ulonglong * 5)()
+        k = self._lib.qses_server_stats(self._h, out, 5)
+        names = ["batches", "served", "max_batch", "max_lanes_busy", "queued"]
+        return {names[i]: int(out[i]) for i in range(k)}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.qses_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass

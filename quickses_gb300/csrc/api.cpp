@@ -8,6 +8,7 @@
 #include <mutex>
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstdint>
 #include <map>
 #include <new>
@@ -416,6 +417,103 @@ QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, uns
             at = end;
         }
     }
+    return QSES_OK;
+}
+
+QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target) {
+    if (!ctx) return QSES_ERR_INVALID_ARG;
+    if (threads == 0) {
+        ctx->gs_force = qses::GsShape{0, 0};
+        return QSES_OK;
+    }
+    if ((threads != 512 && threads != 1024) || target < 256) return QSES_ERR_INVALID_ARG;
+    ctx->gs_force = qses::GsShape{threads, target};
+    return QSES_OK;
+}
+
+QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_float3 *atoms, const float *radii,
+                           unsigned n, int repeats, int *threads_out, unsigned *target_out, float *smooth_ms_out) {
+    if (!ctx || !p || (n && (!atoms || !radii))) return QSES_ERR_INVALID_ARG;
+    int rc = check_params(ctx, p);
+    if (rc) return rc;
+    cudaSetDevice(ctx->device);
+    qses::GsShape cand[16];
+    const int nc = qses::gs_shape_candidates(cand, 16);
+    qses::GsShape best = cand[0];
+    float best_ms = -1.0f;
+    const bool prof = ctx->profiling;
+    ctx->profiling = true;
+    unsigned nv = 0;
+    if (n > 1 && p->smooth_passes > 0) {
+        for (int c = 0; c < nc && rc == QSES_OK; c++) {
+            ctx->gs_force = cand[c];
+            for (int r = 0; r < std::max(1, repeats) && rc == QSES_OK; r++) {
+                if (ctx->input.reserve(16ull * n + 512) != QSES_OK) {
+                    rc = ctx->fail(QSES_ERR_OUT_OF_MEMORY, "input buffers");
+                    break;
+                }
+                float *d_xyz = (float *)ctx->input.take(12ull * n);
+                float *d_r = (float *)ctx->input.take(4ull * n);
+                cudaError_t e = cudaMemcpyAsync(d_xyz, atoms, 12ull * n, cudaMemcpyHostToDevice, ctx->stream);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(d_r, radii, 4ull * n, cudaMemcpyHostToDevice, ctx->stream);
+                if (e != cudaSuccess) {
+                    rc = ctx->fail(QSES_ERR_CUDA, "atom upload", e);
+                    break;
+                }
+                rc = qses::run_pipeline(ctx, *p, d_xyz, d_r, n);
+                if (rc) break;
+                nv = ctx->mesh.nv;
+                for (auto &t : ctx->times)
+                    if (!strcmp(t.first, "smooth") && (best_ms < 0 || t.second < best_ms)) {
+                        best_ms = t.second;
+                        best = cand[c];
+                    }
+            }
+        }
+    }
+    ctx->gs_force = qses::GsShape{0, 0};
+    ctx->profiling = prof;
+    if (rc) return rc;
+    if (nv > 0) qses::gs_shape_record(nv, false, best);
+    if (threads_out) *threads_out = best.threads;
+    if (target_out) *target_out = best.target;
+    if (smooth_ms_out) *smooth_ms_out = best_ms;
+    return QSES_OK;
+}
+
+QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, unsigned count, int repeats,
+                                 int *threads_out, unsigned *target_out, float *ms_out) {
+    if (!ctx || (count && !reqs)) return QSES_ERR_INVALID_ARG;
+    qses::GsShape cand[16];
+    const int nc = qses::gs_shape_candidates(cand, 16);
+    qses::GsShape best = cand[0];
+    double best_s = -1.0;
+    unsigned long long nv = 0;
+    std::vector<qses_mesh> out(count ? count : 1);
+    int rc = QSES_OK;
+    for (int c = 0; c < nc && rc == QSES_OK; c++) {
+        ctx->gs_force = cand[c];
+        for (int r = 0; r < std::max(1, repeats) && rc == QSES_OK; r++) {
+            const auto t0 = std::chrono::steady_clock::now();
+            rc = qses_compute_batch(ctx, reqs, count, out.data(), nullptr);
+            const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            nv = 0;
+            for (unsigned i = 0; i < count; i++) {
+                nv += out[i].n_vertices;
+                qses_mesh_release(&out[i]);
+            }
+            if (rc == QSES_OK && (best_s < 0 || dt < best_s)) {
+                best_s = dt;
+                best = cand[c];
+            }
+        }
+    }
+    ctx->gs_force = qses::GsShape{0, 0};
+    if (rc) return rc;
+    if (nv > 0) qses::gs_shape_record((unsigned)std::min<unsigned long long>(nv, 152ull * qses::kGsSlabMaxVerts), true, best);
+    if (threads_out) *threads_out = best.threads;
+    if (target_out) *target_out = best.target;
+    if (ms_out) *ms_out = (float)(best_s * 1e3);
     return QSES_OK;
 }
 

@@ -68,22 +68,49 @@ __device__ __forceinline__ unsigned sel4(int o, unsigned a, unsigned b, unsigned
     return o == 0 ? a : (o == 1 ? b : (o == 2 ? c : d));
 }
 
-// One warp, one owner row (i, j) of a molecule's grid.  Edge keys get `keyhi` added (the
-// molecule's slot above the local key bits in a batch, 0 for a single molecule).
+// Lanes per owner row: the row's words (voxels 0..Gc) rounded up to a power of two, at
+// most 32, so a warp covers 32 / lanes rows of a small grid at once.
+__host__ __device__ __forceinline__ int mc_lanes(int Gc) {
+    const int Wc = (Gc + 32) / 32;
+    int L = 1;
+    while (L < Wc && L < 32) L <<= 1;
+    return L;
+}
+
+// Sum / inclusive scan over aligned groups of Lg lanes (Lg a power of two, warp-uniform).
+__device__ __forceinline__ unsigned grp_sum(unsigned v, int Lg) {
+    if (Lg == 32) return __reduce_add_sync(0xffffffffu, v);
+    for (int o = Lg >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, Lg);
+    return v;
+}
+__device__ __forceinline__ unsigned grp_incl_scan(unsigned v, int sub, int Lg) {
+    for (int o = 1; o < Lg; o <<= 1) {
+        const unsigned a = __shfl_up_sync(0xffffffffu, v, o, Lg);
+        if (sub >= o) v += a;
+    }
+    return v;
+}
+
+// One owner row (i, j) of a molecule's grid per group of Lg lanes; every lane of the warp
+// calls this (groups whose row is past the end pass valid = false and write nothing).
+// Edge keys get `keyhi` added (the molecule's slot above the local key bits in a batch, 0
+// for a single molecule).
 template <bool EMIT>
-__device__ __forceinline__ void mc_row(const QGrid &g, long long row, const unsigned *__restrict__ sign,
-                                       const unsigned char *__restrict__ codes, const float *lut,
-                                       const unsigned long long *s_tab, uint2 *__restrict__ rowCount,
-                                       const uint2 *__restrict__ rowBase, unsigned *__restrict__ tri,
-                                       unsigned long long *__restrict__ vkey, unsigned long long keyhi) {
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid, int Lg,
+                                       const unsigned *__restrict__ sign, const unsigned char *__restrict__ codes,
+                                       const float *lut, const unsigned long long *s_tab,
+                                       uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
+                                       unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey,
+                                       unsigned long long keyhi) {
+    const int sub = (int)(threadIdx.x & 31) & (Lg - 1);
     const int Gc = g.Gc, E = Gc + 1;
+    if (!valid) row = 0;
     const int i = (int)(row / E), j = (int)(row % E);
-    const bool cellsRow = i < Gc && j < Gc;
+    const bool cellsRow = valid && i < Gc && j < Gc;
     const int Wc = (Gc + 32) / 32;  // words holding voxels 0..Gc
 
     unsigned triBase = 0, eb0 = 0, eb1 = 0, eb2 = 0, eb3 = 0;  // owners (0,0) (0,1) (1,0) (1,1)
-    if (EMIT) {
+    if (EMIT && valid) {
         triBase = rowBase[row].x;
         eb0 = rowBase[row].y;
         if (j + 1 <= Gc) eb1 = rowBase[(size_t)i * E + j + 1].y;
@@ -91,9 +118,9 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, const unsi
         if (i + 1 <= Gc && j + 1 <= Gc) eb3 = rowBase[(size_t)(i + 1) * E + j + 1].y;
     }
     unsigned triCarry = 0, ec0 = 0, ec1 = 0, ec2 = 0, ec3 = 0;
-    for (int w0 = 0; w0 < Wc; w0 += 32) {
-        const int w = w0 + lane;
-        const bool act = w < Wc;
+    for (int w0 = 0; w0 < Wc; w0 += Lg) {
+        const int w = w0 + sub;
+        const bool act = valid && w < Wc;
         const int kb = w * 32;
         unsigned kv = 0u, kc = 0u;
         if (act) {
@@ -122,8 +149,8 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, const unsi
             }
         }
         if (!EMIT) {
-            triCarry += warp_sum(ntri);
-            ec0 += warp_sum(c00);
+            triCarry += grp_sum(ntri, Lg);
+            ec0 += grp_sum(c00, Lg);
             continue;
         }
         // Edges owned by the three neighbouring rows, for triangle corners.
@@ -148,9 +175,9 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, const unsi
         const unsigned xn2 = (nxt && i + 1 < Gc) ? ((N10 ^ N20) & 1u) : 0u, yn2 = (nxt && r2 && j < Gc) ? ((N10 ^ N11) & 1u) : 0u;
         const unsigned xn3 = (nxt && r1 && i + 1 < Gc) ? ((N11 ^ N21) & 1u) : 0u, yn3 = (nxt && r2 && j + 1 < Gc) ? ((N11 ^ N12) & 1u) : 0u;
 
-        const unsigned p0 = warp_incl_scan(c00) - c00, p1 = warp_incl_scan(c01) - c01;
-        const unsigned p2 = warp_incl_scan(c10) - c10, p3 = warp_incl_scan(c11) - c11;
-        const unsigned tp = warp_incl_scan(ntri) - ntri;
+        const unsigned p0 = grp_incl_scan(c00, sub, Lg) - c00, p1 = grp_incl_scan(c01, sub, Lg) - c01;
+        const unsigned p2 = grp_incl_scan(c10, sub, Lg) - c10, p3 = grp_incl_scan(c11, sub, Lg) - c11;
+        const unsigned tp = grp_incl_scan(ntri, sub, Lg) - ntri;
 
         // Vertices owned by this row, in voxel order, x then y then z within a voxel.
         {
@@ -194,13 +221,13 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, const unsi
                 ts += nt;
             }
         }
-        triCarry += warp_sum(ntri);
-        ec0 += warp_sum(c00);
-        ec1 += warp_sum(c01);
-        ec2 += warp_sum(c10);
-        ec3 += warp_sum(c11);
+        triCarry += grp_sum(ntri, Lg);
+        ec0 += grp_sum(c00, Lg);
+        ec1 += grp_sum(c01, Lg);
+        ec2 += grp_sum(c10, Lg);
+        ec3 += grp_sum(c11, Lg);
     }
-    if (!EMIT && lane == 0) rowCount[row] = make_uint2(triCarry, ec0);
+    if (!EMIT && valid && sub == 0) rowCount[row] = make_uint2(triCarry, ec0);
 }
 
 template <bool EMIT>
@@ -213,15 +240,16 @@ __global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict_
     s_tab[threadIdx.x] = c_mc[threadIdx.x];
     if (EMIT) s_lut[threadIdx.x] = lut[threadIdx.x];
     __syncthreads();
-    const int E = g.Gc + 1;
-    const long long row = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (row >= (long long)E * E) return;
-    mc_row<EMIT>(g, row, sign, codes, s_lut, s_tab, rowCount, rowBase, tri, vkey, 0ull);
+    const int E = g.Gc + 1, Lg = mc_lanes(g.Gc);
+    const long long first = ((long long)blockIdx.x * 8 + (threadIdx.x >> 5)) * (32 / Lg), nrow = (long long)E * E;
+    if (first >= nrow) return;  // the whole warp
+    const long long row = first + (threadIdx.x & 31) / Lg;
+    mc_row<EMIT>(g, row, row < nrow, Lg, sign, codes, s_lut, s_tab, rowCount, rowBase, tri, vkey, 0ull);
 }
 
-// Batch form: one warp per owner row of any molecule; rows are numbered molecule after
-// molecule, so one scan over all rows gives every molecule's triangles and edge slots
-// contiguous ranges in molecule order.
+// Batch form: rows are numbered molecule after molecule, so one scan over all rows gives
+// every molecule's triangles and edge slots contiguous ranges in molecule order.  Each warp
+// takes one unit of 32 / Lg rows of one molecule (units numbered by mc_unit_off).
 template <bool EMIT>
 __global__ void __launch_bounds__(256) k_mc_batch(QBatch b, const unsigned *__restrict__ sign,
                                                   const unsigned char *__restrict__ codes, uint2 *__restrict__ rowCount,
@@ -230,14 +258,16 @@ __global__ void __launch_bounds__(256) k_mc_batch(QBatch b, const unsigned *__re
     __shared__ unsigned long long s_tab[256];
     s_tab[threadIdx.x] = c_mc[threadIdx.x];
     __syncthreads();
-    const unsigned row = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (row >= __ldg(b.row_off + b.n_mol)) return;
-    const unsigned m = qses_find(b.row_off, b.n_mol, row);
+    const unsigned unit = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (unit >= __ldg(b.mc_unit_off + b.n_mol)) return;  // the whole warp
+    const unsigned m = qses_find(b.mc_unit_off, b.n_mol, unit);
     const QMol &mol = b.mols[m];
     const QGrid g = mol.g;
-    const unsigned r0 = mol.row_off;
-    mc_row<EMIT>(g, (long long)(row - r0), sign + mol.mask_off, codes + mol.code_off, b.lut + 256ull * m, s_tab,
-                 rowCount + r0, rowBase + r0, tri, vkey, (unsigned long long)m << b.key_bits);
+    const int Lg = mc_lanes(g.Gc);
+    const unsigned r0 = mol.row_off, nrow = (unsigned)(g.Gc + 1) * (unsigned)(g.Gc + 1);
+    const unsigned row = (unit - __ldg(b.mc_unit_off + m)) * (32u / Lg) + (threadIdx.x & 31) / Lg;
+    mc_row<EMIT>(g, (long long)row, row < nrow, Lg, sign + mol.mask_off, codes + mol.code_off, b.lut + 256ull * m,
+                 s_tab, rowCount + r0, rowBase + r0, tri, vkey, (unsigned long long)m << b.key_bits);
 }
 
 // ------------------------------------------------------------------ weld
@@ -527,7 +557,6 @@ __global__ void __launch_bounds__(256) k_gs(float *pos, unsigned nv, const uint2
 // with shared-memory counters and processed in rounds separated by __syncthreads, and only
 // boundary edges go through global memory (an acquire/release counter per vertex and a
 // per-slab inbox).  Each vertex is still computed exactly as the sequential loop would.
-constexpr int kGsT = 512;
 constexpr int kGsSlabMaxSmem = 200 * 1024;  // dynamic part: ring + packed counters, 6 B/vertex
 
 __device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
@@ -603,6 +632,7 @@ __device__ __forceinline__ void ring_push16(volatile unsigned short *ring, unsig
     ring[k] = (unsigned short)off;  // each vertex enters the ring once: no wrap-around
 }
 
+template <int kGsT>
 __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned S,
                                                   const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
                                                   const unsigned short *__restrict__ cnt_local, int *remote,
@@ -785,21 +815,24 @@ __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, uns
 
 static inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
+int mc_rows_per_warp(int Gc) { return 32 / mc_lanes(Gc); }
 void launch_mc_count(const QGrid &g, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
     size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
-    k_mc<false><<<nblk(rows, 8), 256, 0, s>>>(g, sign, nullptr, nullptr, rowCount, nullptr, nullptr, nullptr);
+    k_mc<false><<<nblk(rows, 8 * mc_rows_per_warp(g.Gc)), 256, 0, s>>>(g, sign, nullptr, nullptr, rowCount,
+                                                                          nullptr, nullptr, nullptr);
 }
 void launch_mc_emit(const QGrid &g, const unsigned *sign, const unsigned char *codes, const float *lut,
                     const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s) {
     size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
-    k_mc<true><<<nblk(rows, 8), 256, 0, s>>>(g, sign, codes, lut, nullptr, rowBase, tri, vkey);
+    k_mc<true><<<nblk(rows, 8 * mc_rows_per_warp(g.Gc)), 256, 0, s>>>(g, sign, codes, lut, nullptr, rowBase, tri,
+                                                                         vkey);
 }
-void launch_mc_count_batch(const QBatch &b, unsigned rows, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
-    k_mc_batch<false><<<nblk(rows, 8), 256, 0, s>>>(b, sign, nullptr, rowCount, nullptr, nullptr, nullptr);
+void launch_mc_count_batch(const QBatch &b, unsigned units, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
+    k_mc_batch<false><<<nblk(units, 8), 256, 0, s>>>(b, sign, nullptr, rowCount, nullptr, nullptr, nullptr);
 }
-void launch_mc_emit_batch(const QBatch &b, unsigned rows, const unsigned *sign, const unsigned char *codes,
+void launch_mc_emit_batch(const QBatch &b, unsigned units, const unsigned *sign, const unsigned char *codes,
                           const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s) {
-    k_mc_batch<true><<<nblk(rows, 8), 256, 0, s>>>(b, sign, codes, nullptr, rowBase, tri, vkey);
+    k_mc_batch<true><<<nblk(units, 8), 256, 0, s>>>(b, sign, codes, nullptr, rowBase, tri, vkey);
 }
 void launch_weld_scatter_batch(const QBatch &b, const unsigned long long *skey, const unsigned *sval,
                                const uint2 *excl, unsigned n, unsigned *vmap, float *vq, unsigned *vmol,
@@ -873,20 +906,25 @@ void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s) 
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s) {
     k_from_float4<<<nblk(nv, 256), 256, 0, s>>>(v4, nv, v3);
 }
-cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, const uint2 *start,
-                           const unsigned *nbr, const unsigned short *cnt_local, int *remote, unsigned *inbox,
-                           unsigned *inbox_tail, int *err, long long spin_cycles, unsigned long long *stats,
-                           cudaStream_t s) {
+static const void *gs_flow_fn(int threads) {
+    return threads >= 1024 ? (const void *)k_gs_flow<1024> : (const void *)k_gs_flow<512>;
+}
+cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads,
+                           const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
+                           unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
+                           unsigned long long *stats, cudaStream_t s) {
     size_t smem = gs_slab_smem(S);
-    cudaFuncSetAttribute((const void *)k_gs_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
+    const void *fn = gs_flow_fn(threads);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
     void *args[] = {&pos, &v0, &nv, &S, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
                     &inbox_tail, &err, &spin_cycles, &stats};
-    return cudaLaunchCooperativeKernel((const void *)k_gs_flow, dim3(P), dim3(kGsT), args, smem, s);
+    return cudaLaunchCooperativeKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
 }
-int gs_slab_max_blocks(int device, unsigned S) {
-    cudaFuncSetAttribute((const void *)k_gs_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
+int gs_slab_max_blocks(int device, unsigned S, int threads) {
+    const void *fn = gs_flow_fn(threads);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
     int per_sm = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gs_flow, kGsT, gs_slab_smem(S));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads >= 1024 ? 1024 : 512, gs_slab_smem(S));
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     return per_sm * sms;
 }

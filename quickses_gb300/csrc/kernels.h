@@ -41,11 +41,23 @@ size_t gs_slab_smem(unsigned S);
 void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s);
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s);
 // One Gauss-Seidel pass over vertices [v0, nv) in P slabs of S (no neighbour outside).
-cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, const uint2 *start,
-                           const unsigned *nbr, const unsigned short *cnt_local, int *remote, unsigned *inbox,
-                           unsigned *inbox_tail, int *err, long long spin_cycles, unsigned long long *stats,
-                           cudaStream_t s);
-int gs_slab_max_blocks(int device, unsigned S);
+// threads: 512 or 1024 per slab CTA.
+cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads,
+                           const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
+                           unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
+                           unsigned long long *stats, cudaStream_t s);
+int gs_slab_max_blocks(int device, unsigned S, int threads);
+
+// Gauss-Seidel launch shape: threads per slab CTA and the slab size aimed at (vertices);
+// the result does not depend on it, only the time does.
+struct GsShape {
+    int threads = 512;
+    unsigned target = 16384;
+};
+// Tuned shape for a mesh of nv vertices (batch = waves of many molecules), or the default.
+GsShape gs_shape(unsigned nv, bool batch);
+void gs_shape_record(unsigned nv, bool batch, GsShape s);
+int gs_shape_candidates(GsShape *out, int max);
 constexpr unsigned kGsSlabMaxVerts = 25000;
 
 // ---- batch forms (QBatch: per-molecule grids and offsets in device memory)
@@ -54,8 +66,10 @@ void launch_sas_batch(const QBatch &b, unsigned tiles, const float4 *atoms, cons
                       unsigned *outMask, unsigned *counter, cudaStream_t s);
 void launch_edt_batch(const QBatch &b, unsigned tiles, const unsigned *inMask, const unsigned *outMask,
                       unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s);
-void launch_mc_count_batch(const QBatch &b, unsigned rows, const unsigned *sign, uint2 *rowCount, cudaStream_t s);
-void launch_mc_emit_batch(const QBatch &b, unsigned rows, const unsigned *sign, const unsigned char *codes,
+// Owner rows a marching-cubes warp covers for a grid with Gc emitted cells per axis.
+int mc_rows_per_warp(int Gc);
+void launch_mc_count_batch(const QBatch &b, unsigned units, const unsigned *sign, uint2 *rowCount, cudaStream_t s);
+void launch_mc_emit_batch(const QBatch &b, unsigned units, const unsigned *sign, const unsigned char *codes,
                           const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s);
 void launch_weld_scatter_batch(const QBatch &b, const unsigned long long *skey, const unsigned *sval,
                                const uint2 *excl, unsigned n, unsigned *vmap, float *vq, unsigned *vmol,

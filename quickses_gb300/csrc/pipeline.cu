@@ -111,6 +111,37 @@ void fill_lut(const QGrid &g, float *lut) {
     lut[QSES_CODE_OUT] = g.probe;
 }
 
+// ------------------------------------------------------------------ tuning
+
+// Process-wide Gauss-Seidel shapes per (mode, log2 of the vertex count), filled by the
+// autotuner (qses_autotune*); absent entries use the default shape.
+static std::mutex g_tune_mu;
+static GsShape g_tune[2][33];
+static bool g_tuned[2][33];
+
+static int tune_bucket(unsigned nv) { return bits_for(nv); }
+
+GsShape gs_shape(unsigned nv, bool batch) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const int b = tune_bucket(nv);
+    return g_tuned[batch][b] ? g_tune[batch][b] : GsShape();
+}
+
+void gs_shape_record(unsigned nv, bool batch, GsShape sh) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const int b = tune_bucket(nv);
+    g_tune[batch][b] = sh;
+    g_tuned[batch][b] = true;
+}
+
+int gs_shape_candidates(GsShape *out, int max) {
+    static const GsShape c[] = {{512, 16384}, {1024, 16384}, {512, 8192}, {1024, 8192},
+                                {512, 4096},  {1024, 4096},  {1024, 25000}};
+    int k = 0;
+    for (; k < max && k < (int)(sizeof(c) / sizeof(c[0])); k++) out[k] = c[k];
+    return k;
+}
+
 // ------------------------------------------------------------------ arena
 
 int Arena::reserve(size_t bytes) {
@@ -334,8 +365,10 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         ctx->launches++;
         ctx->mark("smooth_csr");
         // Slab-partitioned exact Gauss-Seidel: P persistent CTAs, contiguous id slabs of S.
-        const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts), 1024);
-        int P = (int)std::min<unsigned>((nv + 16383) / 16384, (unsigned)pmax);
+        const GsShape sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(nv, false);
+        ctx->gs_used = sh;
+        const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts, sh.threads), 1024);
+        int P = (int)std::min<unsigned>((nv + sh.target - 1) / sh.target, (unsigned)pmax);
         if (P < 1) P = 1;
         unsigned S = (nv + P - 1) / P;
         if (S > kGsSlabMaxVerts) {
@@ -352,8 +385,8 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
                 QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
                 unsigned long long *stats = (unsigned long long *)((char *)ctx->small + 256);
                 QCHK(cudaMemsetAsync(stats, 0, 64, s));
-                QCHK(launch_gs_slab(pos4, 0, nv, S, P, deg, nbr, (unsigned short *)cnt, lower, inbox, inbox_tail,
-                                    d_err, 4000000000ll, stats, s));
+                QCHK(launch_gs_slab(pos4, 0, nv, S, P, sh.threads, deg, nbr, (unsigned short *)cnt, lower, inbox,
+                                    inbox_tail, d_err, 4000000000ll, stats, s));
                 ctx->diag[0] = P;
                 ctx->diag[1] = S;
                 ctx->launches++;

@@ -67,8 +67,8 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     // ---- per-molecule layout on the host
     const unsigned nm = count;
     std::vector<QMol> mols(nm);
-    std::vector<unsigned> tile_off(nm + 1), atom_off(nm + 1), row_off(nm + 1);
-    unsigned long long mask_tot = 0, code_tot = 0, cell_tot = 0, tiles = 0, rows = 0, atoms_tot = 0;
+    std::vector<unsigned> tile_off(nm + 1), atom_off(nm + 1), row_off(nm + 1), unit_off(nm + 1);
+    unsigned long long mask_tot = 0, code_tot = 0, cell_tot = 0, tiles = 0, rows = 0, atoms_tot = 0, units = 0;
     for (unsigned m = 0; m < nm; m++) {
         const QGrid &g = items[m].g;
         QMol &q = mols[m];
@@ -83,22 +83,27 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         tile_off[m] = (unsigned)tiles;
         atom_off[m] = (unsigned)atoms_tot;
         row_off[m] = (unsigned)rows;
+        unit_off[m] = (unsigned)units;
         mask_tot += (unsigned long long)g.G * g.G * g.W;
         code_tot += (unsigned long long)g.G * g.G * g.Gp;
         cell_tot += (unsigned long long)g.gnb * g.gnb * g.gnb;
         tiles += (unsigned long long)g.W * ((g.G + 7) / 8) * ((g.G + 7) / 8);
-        rows += (unsigned long long)(g.Gc + 1) * (g.Gc + 1);
+        const unsigned long long r = (unsigned long long)(g.Gc + 1) * (g.Gc + 1);
+        const unsigned long long rpw = (unsigned long long)mc_rows_per_warp(g.Gc);
+        rows += r;
+        units += (r + rpw - 1) / rpw;
         atoms_tot += items[m].n;
     }
     tile_off[nm] = (unsigned)tiles;
     atom_off[nm] = (unsigned)atoms_tot;
     row_off[nm] = (unsigned)rows;
+    unit_off[nm] = (unsigned)units;
     if (tiles >= (1ull << 31) || rows >= (1ull << 31) || cell_tot >= (1ull << 31) || atoms_tot >= (1ull << 30))
         return ctx->fail(QSES_ERR_UNSUPPORTED, "batch too large for 32-bit item indices; split it");
     const unsigned N = (unsigned)atoms_tot;
 
     // ---- pinned staging: descriptor block then atoms, one copy each
-    const size_t desc_bytes = a256(sizeof(QMol) * nm) + 7 * a256(4ull * (nm + 1)) + a256(1024ull * nm);
+    const size_t desc_bytes = a256(sizeof(QMol) * nm) + 8 * a256(4ull * (nm + 1)) + a256(1024ull * nm);
     const size_t atom_bytes = 16ull * N;
     if (stage_reserve(ctx, desc_bytes + atom_bytes + 256) != QSES_OK)
         return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned batch staging");
@@ -113,6 +118,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     hput(tile_off.data(), 4ull * (nm + 1));
     hput(atom_off.data(), 4ull * (nm + 1));
     hput(row_off.data(), 4ull * (nm + 1));
+    hput(unit_off.data(), 4ull * (nm + 1));
     hput(nullptr, 4ull * (nm + 1));  // tri_off   (device-filled)
     hput(nullptr, 4ull * (nm + 1));  // edge_off  (device-filled)
     hput(nullptr, 4ull * (nm + 1));  // vtx_off   (device-filled)
@@ -155,6 +161,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         b.tile_off = (const unsigned *)at(ob);
         b.atom_off = (const unsigned *)at(ob);
         b.row_off = (const unsigned *)at(ob);
+        b.mc_unit_off = (const unsigned *)at(ob);
         b.tri_off = (const unsigned *)at(ob);
         d_edge_off = (unsigned *)at(ob);
         b.vtx_off = (const unsigned *)at(ob);
@@ -201,7 +208,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     ctx->mark("refine");
 
     // ---- marching-cubes counts, one scan over all rows, per-molecule offsets
-    launch_mc_count_batch(b, (unsigned)rows, signMask, rowsb, s);
+    launch_mc_count_batch(b, (unsigned)units, signMask, rowsb, s);
     ctx->launches++;
     QCHK(scan_u2(rowsb, rowsb, (unsigned)rows, d_tot, tmp, d_err, s, &ctx->launches));
     launch_gather_offsets(rowsb, b.row_off, nm, (unsigned)rows, d_tot, d_tri_off, d_edge_off, s);
@@ -249,7 +256,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     if (!tmpb) return ctx->fail(QSES_ERR_INTERNAL, "batch mesh workspace layout");
 
     // ---- triangles + molecule-tagged weld keys, then one weld for all molecules
-    launch_mc_emit_batch(b, (unsigned)rows, signMask, codes, rowsb, tri, vk, s);
+    launch_mc_emit_batch(b, (unsigned)units, signMask, codes, rowsb, tri, vk, s);
     ctx->launches++;
     ctx->mark("mc_emit");
     unsigned nv = 0;
@@ -302,7 +309,9 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         ctx->launches++;
         ctx->mark("smooth_csr");
         // Waves of whole molecules, each at most pmax slabs of kGsSlabMaxVerts vertices.
-        const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts), 1024);
+        const GsShape sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(std::min<unsigned>(nv, 152u * kGsSlabMaxVerts), true);
+        ctx->gs_used = sh;
+        const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts, sh.threads), 1024);
         const unsigned long long cap = (unsigned long long)pmax * kGsSlabMaxVerts;
         std::vector<std::pair<unsigned, unsigned>> waves;
         bool fits = pmax > 0;
@@ -322,7 +331,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
             for (int pass = 0; pass < passes; pass++) {
                 for (auto &w : waves) {
                     const unsigned nw = w.second - w.first;
-                    int P = (int)std::min<unsigned>((nw + 16383) / 16384, (unsigned)pmax);
+                    int P = (int)std::min<unsigned>((nw + sh.target - 1) / sh.target, (unsigned)pmax);
                     if (P < 1) P = 1;
                     unsigned S = (nw + P - 1) / P;
                     if (S > kGsSlabMaxVerts) {
@@ -333,8 +342,8 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
                     ctx->launches++;
                     QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * P * S, s));
                     QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
-                    QCHK(launch_gs_slab(pos4, w.first, w.second, S, P, deg, nbr, (unsigned short *)cnt, lower, inbox,
-                                        inbox_tail, d_err, 4000000000ll, nullptr, s));
+                    QCHK(launch_gs_slab(pos4, w.first, w.second, S, P, sh.threads, deg, nbr, (unsigned short *)cnt,
+                                        lower, inbox, inbox_tail, d_err, 4000000000ll, nullptr, s));
                     ctx->launches++;
                     ctx->diag[0] = std::max<unsigned long long>(ctx->diag[0], (unsigned long long)P);
                 }

@@ -54,6 +54,7 @@ struct QBatch {
     const unsigned *tile_off;  // field tiles (8 x 8 z-rows of 32 voxels) per molecule
     const unsigned *atom_off;
     const unsigned *row_off;
+    const unsigned *mc_unit_off; // marching-cubes warp units (32 / lanes rows each)
     const unsigned *tri_off;   // pre-filter triangles (valid after the row scan)
     const unsigned *vtx_off;   // welded vertices (valid after the weld)
     const float *lut;          // 256 field values per molecule

@@ -8,6 +8,13 @@ minimum pair distance, probe 1.4 A):
 * ``shell1m``   1 000 000 atoms uniform in a 400-430 A shell, voxel 0.5 A, 0 passes
 * ``ball20k``   20 000 atoms, voxel 0.2 A, 1 pass (profiling size: ~127 M voxels, field
                 larger than L2, well under the device memory of a capture)
+
+Request streams for the batch and served forms:
+
+* :func:`uneven_batch`   molecules with atom counts log-uniform in [500, 20 000], voxel 0.4
+* :func:`trajectory`     one 5 000-atom molecule plus i.i.d. N(0, 0.3^2) jitter per frame
+* :func:`served_stream`  atom counts log-uniform in [200, 200 000], voxel one of
+                         {0.3, 0.4, 0.5}; requests draw from a pool of distinct molecules
 """
 import ctypes
 from dataclasses import dataclass
@@ -75,3 +82,31 @@ WORKLOADS = {
     "shell1m": Workload("shell1m", "shell", 1000000, 0.5, 0),
     "ball20k": Workload("ball20k", "ball", 20000, 0.2, 1),
 }
+
+
+def _req(xyz, rad, voxel, smooth=1):
+    return {"xyz": xyz, "radii": rad, "voxel": float(voxel), "smooth": int(smooth), "keep_degenerate": False}
+
+
+def uneven_batch(count=256, seed=2024, lo=500, hi=20000, voxel=0.4):
+    """`count` independent ball molecules, atom counts log-uniform in [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), count)).astype(int)
+    return [_req(*ball(int(n), seed * 1000 + k)[:2], voxel) for k, n in enumerate(sizes)]
+
+
+def trajectory(frames=512, n=5000, sigma=0.3, seed=77, voxel=0.4):
+    """Frames of one molecule: base coordinates plus i.i.d. Gaussian jitter."""
+    base, rad, _ = ball(n, seed)
+    return [_req(jitter(base, sigma, seed * 100000 + f), rad, voxel) for f in range(frames)]
+
+
+def served_stream(count, seed=9, pool=160, lo=200, hi=200000, voxels=(0.3, 0.4, 0.5)):
+    """`count` requests drawn from `pool` distinct molecules (atom counts log-uniform in
+    [lo, hi]), each with a voxel size drawn uniformly from `voxels`."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), pool)).astype(int)
+    mols = [ball(int(n), seed * 10000 + k)[:2] for k, n in enumerate(sizes)]
+    picks = rng.integers(0, pool, count)
+    vox = rng.choice(np.asarray(voxels, np.float64), count)
+    return [_req(mols[p][0], mols[p][1], v) for p, v in zip(picks, vox)]

@@ -88,3 +88,34 @@ def test_multi_wave_smoothing_matches_single(ctx):
     assert sum(len(m.vertices) for m in out) > 152 * 25000
     for r, m in zip(reqs, out):
         _same(m, _single(ctx, r))
+
+
+@pytest.mark.parametrize("threads,target", [(512, 16384), (1024, 16384), (512, 4096), (1024, 4096), (1024, 25000)])
+def test_every_smoothing_shape_is_exact(ctx, threads, target):
+    """The autotuner's candidate launch shapes give the same mesh bit for bit (single and
+    batch), since the Gauss-Seidel order is fixed by the vertex ids."""
+    xyz, rad, _ = q.molecules.ball(3000, 44)
+    ref = O.compute_ses(xyz, rad, 0.3, smooth=2, fp64=False)
+    ctx.set_smoothing_shape(threads, target)
+    try:
+        m = ctx.compute(xyz, rad, voxel=0.3, smooth=2)
+        assert np.array_equal(m.vertices, ref.vertices.astype(np.float32))
+        reqs = [_req(*q.molecules.ball(n, 60 + n)[:2], 0.4, 1) for n in (800, 2500, 6000)]
+        out = ctx.compute_batch(reqs)
+    finally:
+        ctx.set_smoothing_shape(0)
+    for r, mb in zip(reqs, out):
+        _same(mb, _single(ctx, r))
+
+
+def test_autotune_keeps_results(ctx):
+    xyz, rad, _ = q.molecules.ball(2000, 45)
+    before = ctx.compute(xyz, rad, voxel=0.4, smooth=1)
+    threads, target, ms = ctx.autotune(xyz, rad, voxel=0.4, smooth=1)
+    assert threads in (512, 1024) and target >= 256 and ms > 0
+    _same(ctx.compute(xyz, rad, voxel=0.4, smooth=1), before)
+    reqs = [_req(*q.molecules.ball(n, 70 + n)[:2], 0.4, 1) for n in (700, 3000)]
+    singles = [_single(ctx, r) for r in reqs]
+    ctx.autotune_batch(reqs)
+    for m, s1 in zip(ctx.compute_batch(reqs), singles):
+        _same(m, s1)
