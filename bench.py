@@ -30,6 +30,10 @@ sys.path.insert(0, ROOT)
 
 L2_BYTES = 129 * 2 ** 20
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of a stage's kernel, from the
+# ncu capture summarised in the named profile (update both together).
+NCU_TRAFFIC = {}
+
 
 def peaks():
     try:
@@ -153,6 +157,9 @@ def run_gpu(args):
         return ctx.compute_device(d_xyz.data_ptr(), d_rad.data_ptr(), n, voxel=wl.voxel, smooth=wl.smooth)
 
     with torch.cuda.stream(stream):
+        # launch-shape tuning of the smoothing kernel (same mesh for every shape), before
+        # the warm-up: it runs the pipeline once per candidate shape
+        tuned = ctx.autotune(xyz, rad, voxel=wl.voxel, smooth=wl.smooth) if wl.smooth > 0 else None
         for _ in range(args.warmup):
             dm = step()
         torch.cuda.synchronize()
@@ -232,13 +239,17 @@ def run_gpu(args):
                                % (wl.name, n, wl.voxel, wl.smooth, gi.G),
                    "grid_dim": gi.G, "voxels": voxels, "atoms": n, "mesh_vertices": nv, "mesh_triangles": nt,
                    "l2": "flushed between timed steps (256 MB write outside the event pair)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "smoothing_shape": None if tuned is None else
+                   {"threads": tuned[0], "slab_target": tuned[1], "cache_flags": tuned[2]}},
         "e2e": {"value": e2e_value, "unit": "voxels/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "qses_compute (C-ABI, pageable host atoms in, pinned host mesh out)"},
         "roofline": {"kernel": dom[0], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "algorithmic_bytes": nbytes, "stage_ms": dom[1], "traffic": None},
+                     "algorithmic_bytes": nbytes, "stage_ms": dom[1],
+                     "traffic": NCU_TRAFFIC.get((wl.name, dom[0]), {}).get("bytes"),
+                     "traffic_source": NCU_TRAFFIC.get((wl.name, dom[0]), {}).get("source")},
         "stages_ms": {k: round(v, 4) for k, v in stages},
         "gpu_launches": launches * args.steps,
         "smooth_diagnostics": diag,
@@ -261,6 +272,8 @@ def run_once(args):
     wl = q.molecules.WORKLOADS[args.workload]
     xyz, rad, _ = wl.atoms()
     with q.Context(0) as ctx:
+        if args.gs_shape:
+            ctx.set_smoothing_shape(*[int(x) for x in args.gs_shape.split(",")])
         m = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=wl.smooth)
         print(json.dumps({"workload": wl.name, "grid": q.grid_info(xyz, rad, wl.voxel).G,
                           "vertices": len(m.vertices), "triangles": len(m.triangles),
@@ -317,6 +330,148 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+# ------------------------------------------------------------ batch and served forms
+
+def _raw_batch(lib, L, ctx, rr, n):
+    meshes = (L.Mesh * n)()
+    st = (ctypes.c_int * n)()
+    rc = lib.qses_compute_batch(ctx.handle, rr, n, meshes, st)
+    if rc != 0:
+        raise RuntimeError(lib.qses_last_error(ctx.handle).decode())
+    nv = sum(meshes[i].n_vertices for i in range(n))
+    nt = sum(meshes[i].n_triangles for i in range(n))
+    bad = sum(1 for i in range(n) if st[i] != 0)
+    for i in range(n):
+        lib.qses_mesh_release(ctypes.byref(meshes[i]))
+    return nv, nt, bad
+
+
+def _raw_single(lib, L, ctx, reqs):
+    pr = L.Params()
+    lib.qses_params_default(ctypes.byref(pr))
+    m = L.Mesh()
+    for r in reqs:
+        pr.voxel, pr.smooth_passes = r["voxel"], r["smooth"]
+        rc = lib.qses_compute(ctx.handle, ctypes.byref(pr), r["xyz"].ctypes.data_as(ctypes.c_void_p),
+                              r["radii"].ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(r["radii"]),
+                              ctypes.byref(m))
+        if rc != 0:
+            raise RuntimeError(lib.qses_last_error(ctx.handle).decode())
+        lib.qses_mesh_release(ctypes.byref(m))
+
+
+def run_batch_form(args):
+    """Batch form: one step = every molecule of the stream through qses_compute_batch (host
+    atoms in, host meshes out).  Beside it, the same molecules one by one through
+    qses_compute (the plain per-molecule path) on the same GPU."""
+    import quickses_gb300 as q
+    from quickses_gb300 import _lib as L, api as A
+    lib = L.lib()
+    if args.form == "batched":
+        reqs = q.molecules.uneven_batch(256)
+        desc = "256 molecules, atom counts log-uniform in [500, 20000], voxel 0.4 A, 1 pass"
+    else:
+        reqs = q.molecules.trajectory(512)
+        desc = "5000-atom molecule x 512 frames (N(0, 0.3^2) jitter), voxel 0.4 A, 1 pass"
+    n = len(reqs)
+    voxels = float(sum(q.grid_info(r["xyz"], r["radii"], r["voxel"]).G ** 3 for r in reqs))
+    arrays, rr = A._requests(reqs)
+    with q.Context(0) as ctx:
+        tune = ctx.autotune_batch(reqs)  # launch-shape tuning, before the warm-up
+        for _ in range(args.warmup):
+            _raw_batch(lib, L, ctx, rr, n)
+        ctx.set_profiling(True)
+        _raw_batch(lib, L, ctx, rr, n)
+        stages = ctx.stage_times()
+        launches = ctx.last_launch_count()
+        ctx.set_profiling(False)
+        times = []
+        with ClockSampler(0) as clk:
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                nv, nt, bad = _raw_batch(lib, L, ctx, rr, n)
+                times.append(time.perf_counter() - t0)
+        sec = float(np.mean(times))
+        _raw_single(lib, L, ctx, reqs[:8])
+        t0 = time.perf_counter()
+        _raw_single(lib, L, ctx, reqs)
+        t_plain = time.perf_counter() - t0
+    h2d = sum(16 * len(r["radii"]) for r in reqs)
+    d2h = 12 * nv + 12 * nt + 8 * nv
+    print(json.dumps({
+        "metric": "SES molecules/s (%s form)" % args.form, "value": n / sec, "unit": "molecules/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "form": args.form, "molecules": n, "voxels": voxels,
+                   "mesh_vertices": nv, "mesh_triangles": nt, "rejected": bad,
+                   "smoothing_shape": {"threads": tune[0], "slab_target": tune[1], "cache_flags": tune[2]},
+                   "l2": "inputs and meshes far larger than L2"},
+        "voxels_per_s": voxels / sec,
+        "e2e": {"value": n / sec, "unit": "molecules/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "qses_compute_batch (C-ABI, host atoms in, host meshes out)"},
+        "plain_path": {"value": n / t_plain, "unit": "molecules/s",
+                       "path": "the same molecules one by one through qses_compute on the same GPU"},
+        "stages_ms": {k: round(v, 3) for k, v in stages}, "gpu_launches": launches * args.steps,
+        "clocks": clk.summary()}))
+
+
+def run_served_form(args):
+    """Served form: open-loop Poisson arrivals into qses_server (continuous batching over
+    `lanes` streams, 120 GB admission budget); per offered rate, p50/p99 of submit-to-result
+    latency and the completed-request rate.  Requests: atom counts log-uniform in
+    [200, 200000], voxel one of {0.3, 0.4, 0.5} A, 1 pass, drawn from 160 seeded molecules."""
+    import threading
+    import quickses_gb300 as q
+    rates = [float(x) for x in args.rates.split(",")]
+    per_rate = args.requests
+    reqs = q.molecules.served_stream(per_rate * len(rates) + 64)
+    rng = np.random.default_rng(11)
+    sweep = []
+    with q.Server(lanes=args.lanes, memory_budget=120 << 30, max_batch=256) as srv:
+        for r in reqs[-64:]:  # warm-up: workspaces and pinned blocks grow to size once
+            srv.wait(srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"]))
+        with ClockSampler(0) as clk:
+            for ri, rate in enumerate(rates):
+                chunk = reqs[ri * per_rate:(ri + 1) * per_rate]
+                arrivals = np.cumsum(rng.exponential(1.0 / rate, per_rate))
+                tickets = [None] * per_rate
+
+                def submitter():
+                    t0 = time.perf_counter()
+                    for k, r in enumerate(chunk):
+                        d = t0 + arrivals[k] - time.perf_counter()
+                        if d > 0:
+                            time.sleep(d)
+                        tickets[k] = srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"])
+
+                t_start = time.perf_counter()
+                th = threading.Thread(target=submitter)
+                th.start()
+                lat = []
+                for k in range(per_rate):
+                    while tickets[k] is None:
+                        time.sleep(0.0002)
+                    _, info = srv.wait(tickets[k])
+                    lat.append(info["total_s"])
+                t_end = time.perf_counter()
+                th.join()
+                lat = np.array(lat) * 1e3
+                sweep.append({"offered_per_s": rate, "achieved_per_s": per_rate / (t_end - t_start),
+                              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                              "requests": per_rate})
+        stats = srv.stats()
+    best = max(sweep, key=lambda x: x["achieved_per_s"])
+    print(json.dumps({
+        "metric": "SES molecules/s (served form)", "value": best["achieved_per_s"], "unit": "molecules/s",
+        "n_gpus": 1, "steps": len(rates), "warmup": 64, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "open-loop Poisson, %d requests per offered rate, atom counts log-uniform in "
+                               "[200, 200000], voxel one of {0.3, 0.4, 0.5} A, 1 pass" % per_rate,
+                   "form": "served", "lanes": args.lanes, "memory_budget_gb": 120},
+        "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "sweep": sweep, "server": stats,
+        "clocks": clk.summary()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -326,6 +481,13 @@ def main():
     ap.add_argument("--workload", default="ball50k")
     ap.add_argument("--cpu-planes", type=int, default=0, help="x-planes of the CPU sample (0 = whole grid)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", default="plain", choices=["plain", "batched", "trajectory", "served"],
+                    help="plain: one molecule per step (default); batched/trajectory: a molecule stream per step "
+                         "through qses_compute_batch; served: Poisson arrivals into qses_server")
+    ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="served form: offered requests/s")
+    ap.add_argument("--requests", type=int, default=1000, help="served form: requests per offered rate")
+    ap.add_argument("--lanes", type=int, default=2, help="served form: batches in flight")
+    ap.add_argument("--gs-shape", default="", help="profile-once: smoothing shape threads,target,cache_flags")
     ap.add_argument("--profile-once", action="store_true",
                     help="run the pipeline once on the workload (for profiler captures) and exit")
     args = ap.parse_args()
@@ -333,6 +495,10 @@ def main():
         args.warmup = 3
     if args.profile_once:
         run_once(args)
+    elif args.form in ("batched", "trajectory") and args.impl == "ours":
+        run_batch_form(args)
+    elif args.form == "served" and args.impl == "ours":
+        run_served_form(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

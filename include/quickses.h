@@ -166,13 +166,16 @@ QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, uns
  * of the vertex count) use it.  The mesh is identical for every shape: the update order is
  * fixed by the vertex ids.  No reference counterpart (QuickSES hard-codes its launches). */
 QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_float3 *atoms, const float *radii,
-                           unsigned n, int repeats, int *threads_out, unsigned *target_out, float *smooth_ms_out);
-/* Fixes the smoothing launch shape of ctx (threads 512 or 1024 per slab CTA, slab size
- * aimed at >= 256 vertices); threads = 0 returns to the tuned/default shape. */
-QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target);
+                           unsigned n, int repeats, int *threads_out, unsigned *target_out, unsigned *flags_out,
+                           float *smooth_ms_out);
+/* Fixes the smoothing launch shape of ctx: threads 512 or 1024 per slab CTA, slab size
+ * aimed at (>= 256 vertices), cache_flags bit 0 = prefetch successors' neighbour lists into
+ * L1 instead of L2, bit 1 = neighbour positions through L1; threads = 0 returns to the
+ * tuned/default shape.  Every shape gives the same mesh. */
+QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags);
 /* The same for the batch form, timing whole qses_compute_batch calls on `reqs`. */
 QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, unsigned count, int repeats,
-                                 int *threads_out, unsigned *target_out, float *ms_out);
+                                 int *threads_out, unsigned *target_out, unsigned *flags_out, float *ms_out);
 
 /* ---------------------------------------------------------------- served form */
 

@@ -6,6 +6,7 @@ TEST INFRASTRUCTURE ONLY.  Needs oracle/_ref/libQuickSES.so and oracle/_ref/libr
     python oracle/ref_cuda/run_ref.py compare ball1k ball50k   # time + mesh comparison (JSON lines)
     python oracle/ref_cuda/run_ref.py field                    # reference field vs our voxel codes
     python oracle/ref_cuda/run_ref.py fixtures                 # tests/golden/ref_cuda.npz
+    python oracle/ref_cuda/run_ref.py stream batched|trajectory|served   # plain path, molecules/s
 
 Timing is wall clock around the reference's API_computeSES (its whole library call:
 upload, slices, host smoothing, concatenation) and around our qses_compute (upload,
@@ -183,8 +184,31 @@ def fixtures(out=os.path.join(ROOT, "tests", "golden", "ref_cuda.npz")):
     print("wrote", out, os.path.getsize(out))
 
 
+def stream(which, limit=None):
+    """The reference's plain path (one API_computeSES per molecule, wall clock per call) on
+    the request streams of the batch and served forms; prints molecules/s."""
+    streams = {"batched": lambda: q.molecules.uneven_batch(256),
+               "trajectory": lambda: q.molecules.trajectory(512),
+               "served": lambda: q.molecules.served_stream(64)}
+    reqs = streams[which]()
+    if limit:
+        reqs = reqs[:limit]
+    ref = Ref()
+    ref.compute(reqs[0]["xyz"], reqs[0]["radii"], reqs[0]["voxel"], reqs[0]["smooth"])  # warm-up
+    total, vox = 0.0, 0
+    for r in reqs:
+        *_, dt = ref.compute(r["xyz"], r["radii"], r["voxel"], r["smooth"])
+        total += dt
+        vox += q.grid_info(r["xyz"], r["radii"], r["voxel"]).G ** 3
+    print(json.dumps({"stream": which, "molecules": len(reqs), "ref_s": total,
+                      "ref_molecules_per_s": len(reqs) / total, "ref_voxels_per_s": vox / total}), flush=True)
+
+
 if __name__ == "__main__":
     mode = sys.argv[1]
+    if mode == "stream":
+        stream(sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else None)
+        sys.exit(0)
     if mode == "compare":
         compare(sys.argv[2:] or ["ball1k"])
     elif mode == "field":

@@ -82,11 +82,13 @@ SIGNATURES = {
                                            ctypes.POINTER(DeviceMesh)]),
     "qses_compute_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.POINTER(Mesh),
                                           ctypes.POINTER(ctypes.c_int)]),
-    "qses_set_smoothing_shape": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint]),
+    "qses_set_smoothing_shape": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint, ctypes.c_uint]),
     "qses_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _FP, ctypes.c_uint, ctypes.c_int,
-                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint), _FP]),
+                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),
+                                     ctypes.POINTER(ctypes.c_uint), _FP]),
     "qses_autotune_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.c_int,
-                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint), _FP]),
+                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),
+                                           ctypes.POINTER(ctypes.c_uint), _FP]),
     "qses_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
     "qses_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_VP)]),
     "qses_server_submit": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_ulonglong)]),

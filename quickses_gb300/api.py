@@ -153,29 +153,31 @@ class Context:
                 self._lib.qses_mesh_release(ctypes.byref(meshes[i]))
         return out
 
-    def set_smoothing_shape(self, threads=0, target=16384):
-        """Fix the smoothing launch shape (threads 512/1024, slab target); 0 = tuned/default."""
-        self._check(self._lib.qses_set_smoothing_shape(self._h, int(threads), int(target)), "qses_set_smoothing_shape")
+    def set_smoothing_shape(self, threads=0, target=16384, cache_flags=0):
+        """Fix the smoothing launch shape (threads 512/1024, slab target, cache flags);
+        threads 0 = tuned/default."""
+        self._check(self._lib.qses_set_smoothing_shape(self._h, int(threads), int(target), int(cache_flags)),
+                    "qses_set_smoothing_shape")
 
     def autotune(self, xyz, radii, voxel=0.5, smooth=1, repeats=1):
         """Times every smoothing launch shape on this molecule and keeps the fastest for its
         mesh size class; returns (threads, slab target, smoothing ms)."""
         xyz, radii = _f32(xyz, 3), _f32(radii)
-        th, tg, ms = ctypes.c_int(0), ctypes.c_uint(0), ctypes.c_float(0)
+        th, tg, fl, ms = ctypes.c_int(0), ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_float(0)
         rc = self._lib.qses_autotune(self._h, ctypes.byref(self._params(voxel, smooth, False, 300)),
                                      xyz.ctypes.data_as(ctypes.c_void_p),
                                      radii.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), xyz.shape[0], int(repeats),
-                                     ctypes.byref(th), ctypes.byref(tg), ctypes.byref(ms))
+                                     ctypes.byref(th), ctypes.byref(tg), ctypes.byref(fl), ctypes.byref(ms))
         self._check(rc, "qses_autotune")
-        return th.value, tg.value, ms.value
+        return th.value, tg.value, fl.value, ms.value
 
     def autotune_batch(self, requests, repeats=1):
         arrays, reqs = _requests(requests)
-        th, tg, ms = ctypes.c_int(0), ctypes.c_uint(0), ctypes.c_float(0)
+        th, tg, fl, ms = ctypes.c_int(0), ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_float(0)
         rc = self._lib.qses_autotune_batch(self._h, reqs, len(requests), int(repeats), ctypes.byref(th),
-                                           ctypes.byref(tg), ctypes.byref(ms))
+                                           ctypes.byref(tg), ctypes.byref(fl), ctypes.byref(ms))
         self._check(rc, "qses_autotune_batch")
-        return th.value, tg.value, ms.value
+        return th.value, tg.value, fl.value, ms.value
 
     def compute_device(self, d_xyz_ptr, d_radii_ptr, n, voxel=0.5, smooth=1, keep_degenerate=False):
         """Device-resident form (pointers to device float arrays); returns counts and the

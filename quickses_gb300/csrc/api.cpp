@@ -420,25 +420,26 @@ QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, uns
     return QSES_OK;
 }
 
-QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target) {
+QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags) {
     if (!ctx) return QSES_ERR_INVALID_ARG;
     if (threads == 0) {
-        ctx->gs_force = qses::GsShape{0, 0};
+        ctx->gs_force = qses::GsShape{0, 0, 0};
         return QSES_OK;
     }
-    if ((threads != 512 && threads != 1024) || target < 256) return QSES_ERR_INVALID_ARG;
-    ctx->gs_force = qses::GsShape{threads, target};
+    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 3) return QSES_ERR_INVALID_ARG;
+    ctx->gs_force = qses::GsShape{threads, target, cache_flags};
     return QSES_OK;
 }
 
 QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_float3 *atoms, const float *radii,
-                           unsigned n, int repeats, int *threads_out, unsigned *target_out, float *smooth_ms_out) {
+                           unsigned n, int repeats, int *threads_out, unsigned *target_out, unsigned *flags_out,
+                           float *smooth_ms_out) {
     if (!ctx || !p || (n && (!atoms || !radii))) return QSES_ERR_INVALID_ARG;
     int rc = check_params(ctx, p);
     if (rc) return rc;
     cudaSetDevice(ctx->device);
-    qses::GsShape cand[16];
-    const int nc = qses::gs_shape_candidates(cand, 16);
+    qses::GsShape cand[64];
+    const int nc = qses::gs_shape_candidates(cand, 64);
     qses::GsShape best = cand[0];
     float best_ms = -1.0f;
     const bool prof = ctx->profiling;
@@ -471,21 +472,22 @@ QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_f
             }
         }
     }
-    ctx->gs_force = qses::GsShape{0, 0};
+    ctx->gs_force = qses::GsShape{0, 0, 0};
     ctx->profiling = prof;
     if (rc) return rc;
     if (nv > 0) qses::gs_shape_record(nv, false, best);
     if (threads_out) *threads_out = best.threads;
     if (target_out) *target_out = best.target;
+    if (flags_out) *flags_out = best.flags;
     if (smooth_ms_out) *smooth_ms_out = best_ms;
     return QSES_OK;
 }
 
 QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, unsigned count, int repeats,
-                                 int *threads_out, unsigned *target_out, float *ms_out) {
+                                 int *threads_out, unsigned *target_out, unsigned *flags_out, float *ms_out) {
     if (!ctx || (count && !reqs)) return QSES_ERR_INVALID_ARG;
-    qses::GsShape cand[16];
-    const int nc = qses::gs_shape_candidates(cand, 16);
+    qses::GsShape cand[64];
+    const int nc = qses::gs_shape_candidates(cand, 64);
     qses::GsShape best = cand[0];
     double best_s = -1.0;
     unsigned long long nv = 0;
@@ -508,11 +510,12 @@ QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, un
             }
         }
     }
-    ctx->gs_force = qses::GsShape{0, 0};
+    ctx->gs_force = qses::GsShape{0, 0, 0};
     if (rc) return rc;
     if (nv > 0) qses::gs_shape_record((unsigned)std::min<unsigned long long>(nv, 152ull * qses::kGsSlabMaxVerts), true, best);
     if (threads_out) *threads_out = best.threads;
     if (target_out) *target_out = best.target;
+    if (flags_out) *flags_out = best.flags;
     if (ms_out) *ms_out = (float)(best_s * 1e3);
     return QSES_OK;
 }

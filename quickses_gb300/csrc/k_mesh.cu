@@ -95,13 +95,18 @@ __device__ __forceinline__ unsigned grp_incl_scan(unsigned v, int sub, int Lg) {
 // calls this (groups whose row is past the end pass valid = false and write nothing).
 // Edge keys get `keyhi` added (the molecule's slot above the local key bits in a batch, 0
 // for a single molecule).
-template <bool EMIT>
+template <bool EMIT, bool FULL>
 __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid, int Lg,
                                        const unsigned *__restrict__ sign, const unsigned char *__restrict__ codes,
                                        const float *lut, const unsigned long long *s_tab,
                                        uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
                                        unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey,
                                        unsigned long long keyhi) {
+    // FULL: one row per warp (Lg = 32, every group valid), known at compile time.
+    if (FULL) {
+        Lg = 32;
+        valid = true;
+    }
     const int sub = (int)(threadIdx.x & 31) & (Lg - 1);
     const int Gc = g.Gc, E = Gc + 1;
     if (!valid) row = 0;
@@ -230,7 +235,7 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
     if (!EMIT && valid && sub == 0) rowCount[row] = make_uint2(triCarry, ec0);
 }
 
-template <bool EMIT>
+template <bool EMIT, bool FULL>
 __global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict__ sign,
                                             const unsigned char *__restrict__ codes, const float *__restrict__ lut,
                                             uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
@@ -240,11 +245,11 @@ __global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict_
     s_tab[threadIdx.x] = c_mc[threadIdx.x];
     if (EMIT) s_lut[threadIdx.x] = lut[threadIdx.x];
     __syncthreads();
-    const int E = g.Gc + 1, Lg = mc_lanes(g.Gc);
+    const int E = g.Gc + 1, Lg = FULL ? 32 : mc_lanes(g.Gc);
     const long long first = ((long long)blockIdx.x * 8 + (threadIdx.x >> 5)) * (32 / Lg), nrow = (long long)E * E;
     if (first >= nrow) return;  // the whole warp
     const long long row = first + (threadIdx.x & 31) / Lg;
-    mc_row<EMIT>(g, row, row < nrow, Lg, sign, codes, s_lut, s_tab, rowCount, rowBase, tri, vkey, 0ull);
+    mc_row<EMIT, FULL>(g, row, row < nrow, Lg, sign, codes, s_lut, s_tab, rowCount, rowBase, tri, vkey, 0ull);
 }
 
 // Batch form: rows are numbered molecule after molecule, so one scan over all rows gives
@@ -266,8 +271,14 @@ __global__ void __launch_bounds__(256) k_mc_batch(QBatch b, const unsigned *__re
     const int Lg = mc_lanes(g.Gc);
     const unsigned r0 = mol.row_off, nrow = (unsigned)(g.Gc + 1) * (unsigned)(g.Gc + 1);
     const unsigned row = (unit - __ldg(b.mc_unit_off + m)) * (32u / Lg) + (threadIdx.x & 31) / Lg;
-    mc_row<EMIT>(g, (long long)row, row < nrow, Lg, sign + mol.mask_off, codes + mol.code_off, b.lut + 256ull * m,
-                 s_tab, rowCount + r0, rowBase + r0, tri, vkey, (unsigned long long)m << b.key_bits);
+    if (Lg == 32)  // warp-uniform
+        mc_row<EMIT, true>(g, (long long)row, true, 32, sign + mol.mask_off, codes + mol.code_off,
+                           b.lut + 256ull * m, s_tab, rowCount + r0, rowBase + r0, tri, vkey,
+                           (unsigned long long)m << b.key_bits);
+    else
+        mc_row<EMIT, false>(g, (long long)row, row < nrow, Lg, sign + mol.mask_off, codes + mol.code_off,
+                            b.lut + 256ull * m, s_tab, rowCount + r0, rowBase + r0, tri, vkey,
+                            (unsigned long long)m << b.key_bits);
 }
 
 // ------------------------------------------------------------------ weld
@@ -632,22 +643,37 @@ __device__ __forceinline__ void ring_push16(volatile unsigned short *ring, unsig
     ring[k] = (unsigned short)off;  // each vertex enters the ring once: no wrap-around
 }
 
-template <int kGsT>
+constexpr unsigned kGsOutbox = 1024;  // shared-memory queue of cross-slab releases
+
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+// Warp roles: warp 0 takes boundary arrivals from lower slabs, warp 1 sends this slab's
+// cross-slab releases (GPU-scope atomics, off the workers' critical path), the other warps
+// update vertices.
+template <int kGsT, unsigned kFlags>
 __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned S,
                                                   const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
                                                   const unsigned short *__restrict__ cnt_local, int *remote,
                                                   unsigned *inbox, unsigned *inbox_tail, int *err,
                                                   long long spin_cycles, unsigned long long *stats) {
     extern __shared__ unsigned s_dyn[];
-    __shared__ unsigned s_head, s_tail, s_done, s_seen, s_stop;
+    __shared__ unsigned s_head, s_tail, s_done, s_seen, s_stop, s_ob_head, s_ob_tail;
+    __shared__ unsigned s_ob[kGsOutbox];
     const unsigned p = blockIdx.x, a = v0 + p * S;  // vertices [v0, nv) in slabs of S
     if (a >= nv) return;  // uniform per CTA
     const unsigned b = min(a + S, nv), len = b - a;
     unsigned *st = s_dyn;                                        // len + 1 CSR offsets of the slab
     unsigned *cnt = s_dyn + (S + 1);                             // (len + 1) / 2 words: packed counters
     volatile unsigned short *ring = (volatile unsigned short *)(cnt + (S + 1) / 2);  // slab offsets
+    volatile unsigned *ob = s_ob;
     unsigned *box = inbox + (a - v0);                            // boundary arrivals from lower slabs
-    if (threadIdx.x == 0) { s_head = 0; s_tail = 0; s_done = 0; s_seen = 0; s_stop = 0; }
+    if (threadIdx.x == 0) { s_head = 0; s_tail = 0; s_done = 0; s_seen = 0; s_stop = 0; s_ob_head = 0; s_ob_tail = 0; }
+    for (unsigned k = threadIdx.x; k < kGsOutbox; k += kGsT) s_ob[k] = 0xffffffffu;
     for (unsigned k = threadIdx.x; k <= len; k += kGsT) st[k] = start[a + k].x;
     for (unsigned k = threadIdx.x; k < len; k += kGsT) ring[k] = 0xffffu;
     for (unsigned k = threadIdx.x; 2 * k < len; k += kGsT) {
@@ -694,6 +720,49 @@ __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, uns
                 if (tail == seen) __nanosleep(20);
             }
         }
+    } else if (threadIdx.x < 64) {
+        // Warp 1 sends cross-slab releases queued by the workers, up to 32 at a time.  A
+        // worker queues an entry after its position store and a CTA-scope fence; the fence
+        // here plus the GPU-scope acq_rel atomic carry that store to the receiving slab.
+        unsigned head = 0;
+        for (;;) {
+            const unsigned tail = *(volatile unsigned *)&s_ob_tail;
+            const unsigned count = min(tail - head, 32u);
+            if (count == 0) {
+                if (*(volatile unsigned *)&s_stop) break;
+                if (*(volatile unsigned *)&s_done >= len) {
+                    __threadfence_block();
+                    if (*(volatile unsigned *)&s_ob_tail == head) break;  // every worker is done
+                    continue;
+                }
+                __nanosleep(20);
+                continue;
+            }
+            if (lane < count) {
+                volatile unsigned *slot = ob + (head + lane) % kGsOutbox;
+                unsigned u = 0xffffffffu;
+                for (unsigned it = 0; it < (1u << 20) && u == 0xffffffffu; it++) u = *slot;  // reserved slot
+                if (u == 0xffffffffu || u < b || u >= nv) {
+                    raise_error(err, u == 0xffffffffu ? QSES_ERR_TIMEOUT : QSES_ERR_INTERNAL);
+                    s_stop = 1;
+                } else {
+                    *slot = 0xffffffffu;
+                    __threadfence_block();
+                    if (atom_sub_acq_rel(remote + u, 1) == 1) {
+                        // last lower-slab dependency of u: hand u to its slab
+                        const unsigned qs = (u - v0) / S;
+                        const unsigned k = atomicAdd(inbox_tail + qs, 1u);
+                        if (k < S) st_release_u32(inbox + (size_t)qs * S + k, u);
+                    }
+                }
+            }
+            head += count;
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
+                *(volatile unsigned *)&s_ob_head = head;  // slots before head are free again
+            }
+        }
     } else {
         // Worker warps: one vertex per warp; lanes fetch neighbours in parallel.
         for (;;) {
@@ -730,7 +799,8 @@ __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, uns
                     const unsigned m = min(32u, e1 - base);
                     const unsigned id = lane < m ? __ldg(nbr + base + lane) : v;
                     if (base == e0) first_id = id;
-                    const float4 q = __ldcg(pos4 + id);
+                    // Weak loads either way: the CTA- and GPU-scope acquires above order them.
+                    const float4 q = (kFlags & kGsL1Positions) ? pos4[id] : __ldcg(pos4 + id);
                     // strictly in neighbour-list order; lanes past m add +0.0f (a sum that
                     // started at +0.0f is unchanged by it)
                     const float qx = lane < m ? q.x : 0.0f, qy = lane < m ? q.y : 0.0f, qz = lane < m ? q.z : 0.0f;
@@ -750,17 +820,13 @@ __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, uns
                     }
                 }
                 const float n = (float)(int)(e1 - e0);
-                if (lane == 0) __stcg(pos4 + v, make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f));
-                const long long c1 = clock64();
-                // The new position must be visible before any successor can start: CTA scope
-                // inside the slab, GPU scope when a hand-off to a higher slab may follow.
-                const unsigned m0 = min(32u, e1 - e0);
-                const bool remote_any = __any_sync(0xffffffffu, lane < m0 && first_id > v && first_id >= b) ||
-                                        (e1 - e0 > 32);
                 if (lane == 0) {
-                    if (remote_any) __threadfence();
-                    else __threadfence_block();
+                    __stcg(pos4 + v, make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f));
+                    // Successors in this slab read the new position after a CTA-scope
+                    // acquire; successors in higher slabs get it through the sender warp.
+                    __threadfence_block();
                 }
+                const long long c1 = clock64();
                 __syncwarp();
                 // Release: one lane per neighbour entry.
                 unsigned next = 0xffffffffu;
@@ -772,12 +838,22 @@ __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, uns
                     bool ready = false;
                     if (higher) {
                         if (!remote_edge) {
+                            // u's list, needed when u runs
+                            if (kFlags & kGsL1Prefetch) prefetch_l1(nbr + st[u - a]);
+                            else prefetch_l2(nbr + st[u - a]);
                             ready = dec16(cnt, u - a) == 1u;
-                        } else if (atom_sub_acq_rel(remote + u, 1) == 1) {
-                            // last lower-slab dependency of u: hand u to its slab
-                            const unsigned qs = (u - v0) / S;
-                            const unsigned k = atomicAdd(inbox_tail + qs, 1u);
-                            if (k < S) st_release_u32(inbox + (size_t)qs * S + k, u);
+                        } else {
+                            const unsigned k = atomicAdd(&s_ob_tail, 1u);
+                            unsigned it = 0;
+                            for (; it < (1u << 22) && k - *(volatile unsigned *)&s_ob_head >= kGsOutbox; it++)
+                                __nanosleep(32);
+                            if (k - *(volatile unsigned *)&s_ob_head >= kGsOutbox) {
+                                raise_error(err, QSES_ERR_TIMEOUT);
+                                s_stop = 1;
+                            } else {
+                                __threadfence_block();  // release: the position store before the entry
+                                ob[k % kGsOutbox] = u;
+                            }
                         }
                     }
                     unsigned mask = __ballot_sync(0xffffffffu, ready);
@@ -788,6 +864,7 @@ __global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, uns
                     }
                     if ((mask >> lane) & 1u) ring_push16(ring, &s_tail, u - a);
                 }
+                __syncwarp();  // queued releases precede the done count the sender checks
                 if (lane == 0) atomicAdd(&s_done, 1u);
                 v = next;
                 const long long c2 = clock64();
@@ -818,14 +895,21 @@ static inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1
 int mc_rows_per_warp(int Gc) { return 32 / mc_lanes(Gc); }
 void launch_mc_count(const QGrid &g, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
     size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
-    k_mc<false><<<nblk(rows, 8 * mc_rows_per_warp(g.Gc)), 256, 0, s>>>(g, sign, nullptr, nullptr, rowCount,
-                                                                          nullptr, nullptr, nullptr);
+    if (mc_lanes(g.Gc) == 32)
+        k_mc<false, true><<<nblk(rows, 8), 256, 0, s>>>(g, sign, nullptr, nullptr, rowCount, nullptr, nullptr,
+                                                         nullptr);
+    else
+        k_mc<false, false><<<nblk(rows, 8 * mc_rows_per_warp(g.Gc)), 256, 0, s>>>(g, sign, nullptr, nullptr,
+                                                                                 rowCount, nullptr, nullptr, nullptr);
 }
 void launch_mc_emit(const QGrid &g, const unsigned *sign, const unsigned char *codes, const float *lut,
                     const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s) {
     size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
-    k_mc<true><<<nblk(rows, 8 * mc_rows_per_warp(g.Gc)), 256, 0, s>>>(g, sign, codes, lut, nullptr, rowBase, tri,
-                                                                         vkey);
+    if (mc_lanes(g.Gc) == 32)
+        k_mc<true, true><<<nblk(rows, 8), 256, 0, s>>>(g, sign, codes, lut, nullptr, rowBase, tri, vkey);
+    else
+        k_mc<true, false><<<nblk(rows, 8 * mc_rows_per_warp(g.Gc)), 256, 0, s>>>(g, sign, codes, lut, nullptr,
+                                                                                rowBase, tri, vkey);
 }
 void launch_mc_count_batch(const QBatch &b, unsigned units, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
     k_mc_batch<false><<<nblk(units, 8), 256, 0, s>>>(b, sign, nullptr, rowCount, nullptr, nullptr, nullptr);
@@ -906,22 +990,27 @@ void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s) 
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s) {
     k_from_float4<<<nblk(nv, 256), 256, 0, s>>>(v4, nv, v3);
 }
-static const void *gs_flow_fn(int threads) {
-    return threads >= 1024 ? (const void *)k_gs_flow<1024> : (const void *)k_gs_flow<512>;
+static const void *gs_flow_fn(int threads, unsigned flags) {
+    static const void *fn[2][4] = {
+        {(const void *)k_gs_flow<512, 0>, (const void *)k_gs_flow<512, 1>, (const void *)k_gs_flow<512, 2>,
+         (const void *)k_gs_flow<512, 3>},
+        {(const void *)k_gs_flow<1024, 0>, (const void *)k_gs_flow<1024, 1>, (const void *)k_gs_flow<1024, 2>,
+         (const void *)k_gs_flow<1024, 3>}};
+    return fn[threads >= 1024 ? 1 : 0][flags & 3u];
 }
-cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads,
+cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads, unsigned flags,
                            const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
                            unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
                            unsigned long long *stats, cudaStream_t s) {
     size_t smem = gs_slab_smem(S);
-    const void *fn = gs_flow_fn(threads);
+    const void *fn = gs_flow_fn(threads, flags);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
     void *args[] = {&pos, &v0, &nv, &S, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
                     &inbox_tail, &err, &spin_cycles, &stats};
     return cudaLaunchCooperativeKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
 }
 int gs_slab_max_blocks(int device, unsigned S, int threads) {
-    const void *fn = gs_flow_fn(threads);
+    const void *fn = gs_flow_fn(threads, 0);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
     int per_sm = 0, sms = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads >= 1024 ? 1024 : 512, gs_slab_smem(S));

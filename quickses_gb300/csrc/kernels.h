@@ -42,7 +42,7 @@ void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s);
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s);
 // One Gauss-Seidel pass over vertices [v0, nv) in P slabs of S (no neighbour outside).
 // threads: 512 or 1024 per slab CTA.
-cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads,
+cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads, unsigned flags,
                            const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
                            unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
                            unsigned long long *stats, cudaStream_t s);
@@ -53,7 +53,11 @@ int gs_slab_max_blocks(int device, unsigned S, int threads);
 struct GsShape {
     int threads = 512;
     unsigned target = 16384;
+    unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions
 };
+// Cache policies of the smoothing kernel (same results, different memory paths):
+constexpr unsigned kGsL1Prefetch = 1;   // prefetch a successor's neighbour list into L1, not L2
+constexpr unsigned kGsL1Positions = 2;  // neighbour positions through L1 (default: L2 only)
 // Tuned shape for a mesh of nv vertices (batch = waves of many molecules), or the default.
 GsShape gs_shape(unsigned nv, bool batch);
 void gs_shape_record(unsigned nv, bool batch, GsShape s);

@@ -135,10 +135,12 @@ void gs_shape_record(unsigned nv, bool batch, GsShape sh) {
 }
 
 int gs_shape_candidates(GsShape *out, int max) {
-    static const GsShape c[] = {{512, 16384}, {1024, 16384}, {512, 8192}, {1024, 8192},
-                                {512, 4096},  {1024, 4096},  {1024, 25000}};
+    static const unsigned targets[] = {4096, 8192, 16384, 25000};
     int k = 0;
-    for (; k < max && k < (int)(sizeof(c) / sizeof(c[0])); k++) out[k] = c[k];
+    for (int t : {512, 1024})
+        for (unsigned tg : targets)
+            for (unsigned f = 0; f < 4; f++)
+                if (k < max) out[k++] = GsShape{t, tg, f};
     return k;
 }
 
@@ -385,7 +387,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
                 QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
                 unsigned long long *stats = (unsigned long long *)((char *)ctx->small + 256);
                 QCHK(cudaMemsetAsync(stats, 0, 64, s));
-                QCHK(launch_gs_slab(pos4, 0, nv, S, P, sh.threads, deg, nbr, (unsigned short *)cnt, lower, inbox,
+                QCHK(launch_gs_slab(pos4, 0, nv, S, P, sh.threads, sh.flags, deg, nbr, (unsigned short *)cnt, lower, inbox,
                                     inbox_tail, d_err, 4000000000ll, stats, s));
                 ctx->diag[0] = P;
                 ctx->diag[1] = S;

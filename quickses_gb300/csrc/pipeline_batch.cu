@@ -342,7 +342,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
                     ctx->launches++;
                     QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * P * S, s));
                     QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
-                    QCHK(launch_gs_slab(pos4, w.first, w.second, S, P, sh.threads, deg, nbr, (unsigned short *)cnt,
+                    QCHK(launch_gs_slab(pos4, w.first, w.second, S, P, sh.threads, sh.flags, deg, nbr, (unsigned short *)cnt,
                                         lower, inbox, inbox_tail, d_err, 4000000000ll, nullptr, s));
                     ctx->launches++;
                     ctx->diag[0] = std::max<unsigned long long>(ctx->diag[0], (unsigned long long)P);

@@ -76,7 +76,7 @@ struct qses_context {
     std::vector<std::pair<const char *, cudaEvent_t>> marks;
     std::vector<std::pair<const char *, float>> times;
     int launches = 0;
-    qses::GsShape gs_force{0, 0};     // autotuner: forced smoothing shape (threads 0 = none)
+    qses::GsShape gs_force{0, 0, 0};  // autotuner: forced smoothing shape (threads 0 = none)
     qses::GsShape gs_used;            // shape of the last smoothing run
     unsigned long long diag[8] = {0};  // smoothing diagnostics: slabs, slab size, max/idle/total rounds
 

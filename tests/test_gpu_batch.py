@@ -90,13 +90,14 @@ def test_multi_wave_smoothing_matches_single(ctx):
         _same(m, _single(ctx, r))
 
 
-@pytest.mark.parametrize("threads,target", [(512, 16384), (1024, 16384), (512, 4096), (1024, 4096), (1024, 25000)])
-def test_every_smoothing_shape_is_exact(ctx, threads, target):
-    """The autotuner's candidate launch shapes give the same mesh bit for bit (single and
-    batch), since the Gauss-Seidel order is fixed by the vertex ids."""
+@pytest.mark.parametrize("threads,target,flags", [(512, 16384, 0), (1024, 16384, 0), (512, 4096, 1), (1024, 4096, 2),
+                                                  (1024, 25000, 3), (512, 8192, 3)])
+def test_every_smoothing_shape_is_exact(ctx, threads, target, flags):
+    """The autotuner's candidate launch shapes and cache policies give the same mesh bit
+    for bit (single and batch), since the Gauss-Seidel order is fixed by the vertex ids."""
     xyz, rad, _ = q.molecules.ball(3000, 44)
     ref = O.compute_ses(xyz, rad, 0.3, smooth=2, fp64=False)
-    ctx.set_smoothing_shape(threads, target)
+    ctx.set_smoothing_shape(threads, target, flags)
     try:
         m = ctx.compute(xyz, rad, voxel=0.3, smooth=2)
         assert np.array_equal(m.vertices, ref.vertices.astype(np.float32))
@@ -111,8 +112,8 @@ def test_every_smoothing_shape_is_exact(ctx, threads, target):
 def test_autotune_keeps_results(ctx):
     xyz, rad, _ = q.molecules.ball(2000, 45)
     before = ctx.compute(xyz, rad, voxel=0.4, smooth=1)
-    threads, target, ms = ctx.autotune(xyz, rad, voxel=0.4, smooth=1)
-    assert threads in (512, 1024) and target >= 256 and ms > 0
+    threads, target, flags, ms = ctx.autotune(xyz, rad, voxel=0.4, smooth=1)
+    assert threads in (512, 1024) and target >= 256 and 0 <= flags <= 3 and ms > 0
     _same(ctx.compute(xyz, rad, voxel=0.4, smooth=1), before)
     reqs = [_req(*q.molecules.ball(n, 70 + n)[:2], 0.4, 1) for n in (700, 3000)]
     singles = [_single(ctx, r) for r in reqs]

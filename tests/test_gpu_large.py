@@ -54,6 +54,17 @@ def test_smoothing_at_scale_exact(big):
     assert np.array_equal(m1.triangles, m0.triangles)
 
 
+@pytest.mark.parametrize("threads,target,flags", [(1024, 16384, 0), (1024, 4096, 3), (512, 25000, 2)])
+def test_smoothing_shapes_at_scale_exact(big, threads, target, flags):
+    """~150 slabs, every cache policy: still the sequential Gauss-Seidel result."""
+    xyz, rad, _, m0, _, _, _ = big
+    ref = O.smooth_f32(m0.vertices, m0.triangles, 1)
+    with q.Context(0) as c:
+        c.set_smoothing_shape(threads, target, flags)
+        m = c.compute(xyz, rad, voxel=WL.voxel, smooth=1, keep_degenerate=True)
+    assert np.array_equal(m.vertices, ref)
+
+
 def test_mesh_properties(big):
     _, _, g, m0, _, _, m1k = big
     v = m0.vertices.astype(np.float64)
