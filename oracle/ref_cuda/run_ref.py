@@ -96,6 +96,31 @@ def mesh_distances(va, ta, vb, tb, dx):
             "frac_ours_within_0.05dx": float(np.mean(d_ba <= tol))}
 
 
+def seam_split(va, ta, vb, tb, g, slice_=300, band=None):
+    """Distances from mesh a's used vertices to mesh b, split by whether the vertex lies in
+    a seam band of the reference's slicing (within R + 2 voxels of a slice-core boundary,
+    CudaSurf.cu:653-682) or away from every seam."""
+    S = min(slice_, g.G)
+    band = band if band is not None else g.R + 2
+    keep = np.zeros(len(va), bool)
+    keep[ta.ravel()] = True
+    pts = va[keep].astype(np.float64)
+    c = (pts - np.array([g.ox, g.oy, g.oz])) / g.dx
+    planes = np.arange(S, g.G, S, dtype=np.float64)
+    if len(planes) == 0:
+        in_band = np.zeros(len(pts), bool)
+    else:
+        dist = np.min(np.abs(c[:, :, None] - planes[None, None, :]), axis=2)
+        in_band = (dist <= band).any(axis=1)
+    d = O.point_surface(pts, vb.astype(np.float64), tb)
+    out = {"seam_band_voxels": band, "vertices_in_band": int(in_band.sum()), "vertices_off_band": int((~in_band).sum())}
+    for name, m in (("off_band", ~in_band), ("in_band", in_band)):
+        if m.any():
+            out["max_%s_A" % name] = float(d[m].max())
+            out["p999_%s_A" % name] = float(np.percentile(d[m], 99.9))
+    return out
+
+
 def vertex_set_overlap(vr, ar, vo, ao):
     """Unsmoothed meshes: exact position matches and closest-atom agreement on them."""
     kr = {tuple(p): i for i, p in enumerate(vr.tolist())}
@@ -125,6 +150,12 @@ def compare(names):
                    "ref_vertices": len(vr), "ref_triangles": len(tr),
                    "our_vertices": len(mo.vertices), "our_triangles": len(mo.triangles)}
             res.update(mesh_distances(vr, tr, mo.vertices, mo.triangles, wl.voxel))
+            if G > 300:  # several reference slices: seam bands vs the rest, unsmoothed and smoothed
+                g, _ = O.grid(xyz, rad, wl.voxel)
+                vr0, tr0, _, _ = ref.compute(xyz, rad, wl.voxel, 0)
+                mo0 = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=0)
+                res["ref_to_ours_unsmoothed"] = seam_split(vr0, tr0, mo0.vertices, mo0.triangles, g)
+                res["ref_to_ours_smoothed"] = seam_split(vr, tr, mo.vertices, mo.triangles, g)
             if G <= 300:  # one reference slice: unsmoothed vertex sets are comparable one to one
                 vr0, tr0, ar0, _ = ref.compute(xyz, rad, wl.voxel, 0)
                 mo0 = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=0)
