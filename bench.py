@@ -462,6 +462,14 @@ def run_served_form(args):
                               "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                               "requests": per_rate})
         stats = srv.stats()
+    # the plain per-request path on the same GPU: one qses_compute at a time, closed loop
+    from quickses_gb300 import _lib as L
+    sample = reqs[:96]
+    with q.Context(0) as ctx:
+        _raw_single(L.lib(), L, ctx, sample[:8])
+        t0 = time.perf_counter()
+        _raw_single(L.lib(), L, ctx, sample)
+        plain = len(sample) / (time.perf_counter() - t0)
     best = max(sweep, key=lambda x: x["achieved_per_s"])
     print(json.dumps({
         "metric": "SES molecules/s (served form)", "value": best["achieved_per_s"], "unit": "molecules/s",
@@ -471,6 +479,8 @@ def run_served_form(args):
                                "[200, 200000], voxel one of {0.3, 0.4, 0.5} A, 1 pass" % per_rate,
                    "form": "served", "lanes": args.lanes, "memory_budget_gb": 120},
         "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "sweep": sweep, "server": stats,
+        "plain_path": {"value": plain, "unit": "molecules/s",
+                       "path": "the first %d requests one by one through qses_compute on the same GPU" % len(sample)},
         "clocks": clk.summary()}))
 
 

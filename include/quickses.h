@@ -158,6 +158,10 @@ typedef struct {
 QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, unsigned count, qses_mesh *out,
                                 int *status);
 
+/* Pinned host memory kept for reuse by released meshes (default 16 GB): result buffers are
+ * pinned for full-speed copies, and pinning is slow, so released blocks are cached. */
+QSES_API void qses_set_pinned_cache(unsigned long long bytes);
+
 /* ------------------------------------------------------------------ autotuner */
 
 /* Picks the smoothing launch shape (threads per slab CTA, slab size aimed at) for meshes of
@@ -190,6 +194,9 @@ typedef struct {
     int lanes;                         /* batches in flight (default 2) */
     unsigned long long memory_budget;  /* device bytes for admitted work (default 120 GB) */
     unsigned max_batch;                /* requests per batch (default 256) */
+    unsigned long long max_batch_voxels; /* grid voxels per batch, summed (default 1e9; 0 = no
+                                            limit): bounds a batch's run time, so lanes take
+                                            turns and late arrivals wait less */
 } qses_server_config;
 typedef struct {
     double queued_s;  /* submit -> start of its batch */

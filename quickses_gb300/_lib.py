@@ -48,7 +48,7 @@ class Request(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("lanes", ctypes.c_int), ("memory_budget", ctypes.c_ulonglong),
-                ("max_batch", ctypes.c_uint)]
+                ("max_batch", ctypes.c_uint), ("max_batch_voxels", ctypes.c_ulonglong)]
 
 
 class TicketInfo(ctypes.Structure):
@@ -82,6 +82,7 @@ SIGNATURES = {
                                            ctypes.POINTER(DeviceMesh)]),
     "qses_compute_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.POINTER(Mesh),
                                           ctypes.POINTER(ctypes.c_int)]),
+    "qses_set_pinned_cache": (None, [ctypes.c_ulonglong]),
     "qses_set_smoothing_shape": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint, ctypes.c_uint]),
     "qses_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _FP, ctypes.c_uint, ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),

@@ -320,11 +320,13 @@ class Server:
     device-memory budget.  submit() copies the atoms and returns a ticket; wait() returns
     (Mesh, timing) for it, or raises QSESError with the request's status."""
 
-    def __init__(self, device=0, lanes=2, memory_budget=120 << 30, max_batch=256):
+    def __init__(self, device=0, lanes=2, memory_budget=120 << 30, max_batch=256, max_batch_voxels=None):
         self._lib = L.lib()
         cfg = L.ServerConfig()
         self._lib.qses_server_config_default(ctypes.byref(cfg))
         cfg.device, cfg.lanes, cfg.memory_budget, cfg.max_batch = device, lanes, memory_budget, max_batch
+        if max_batch_voxels is not None:
+            cfg.max_batch_voxels = int(max_batch_voxels)
         h = ctypes.c_void_p()
         rc = self._lib.qses_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != L.QSES_OK:

@@ -69,7 +69,7 @@ class PinnedPool {
     void give(void *p, size_t bytes) {
         {
             std::lock_guard<std::mutex> lock(mu_);
-            if (cached_ + bytes <= kCap) {
+            if (cached_ + bytes <= cap_) {
                 free_.emplace_back(p, bytes);
                 cached_ += bytes;
                 return;
@@ -79,7 +79,18 @@ class PinnedPool {
     }
 
   private:
-    static constexpr size_t kCap = 4ull << 30;  // pinned bytes kept for reuse
+    size_t cap_ = 16ull << 30;  // pinned bytes kept for reuse (qses_set_pinned_cache)
+
+  public:
+    void set_cap(size_t bytes) {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            cap_ = bytes;
+        }
+        trim(bytes);
+    }
+
+  private:
     // size classes: 64 KB granularity below 1 MB, then 1/8 steps of the next power of two
     static size_t size_class(size_t b) {
         if (b <= (1u << 20)) return (b + 65535) & ~(size_t)65535;
@@ -419,6 +430,8 @@ QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, uns
     }
     return QSES_OK;
 }
+
+QSES_API void qses_set_pinned_cache(unsigned long long bytes) { pinned_pool().set_cap((size_t)bytes); }
 
 QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags) {
     if (!ctx) return QSES_ERR_INVALID_ARG;

@@ -32,6 +32,7 @@ struct Job {
     std::vector<float> xyz, r;
     qses_request req;
     unsigned long long est_bytes = 0;
+    unsigned long long voxels = 0;   // G^3: the work estimate used to bound a batch
     int status = QSES_OK;
     qses_mesh mesh;
     bool done = false;
@@ -77,11 +78,14 @@ void qses_server::lane_loop(int lane) {
             std::unique_lock<std::mutex> lock(mu);
             cv_work.wait(lock, [&] { return stopping || !pending.empty(); });
             if (stopping && pending.empty()) return;
-            unsigned long long bytes = 0;
+            unsigned long long bytes = 0, vox = 0;
             while (!pending.empty() && batch.size() < cfg.max_batch) {
                 Job *j = pending.front();
-                if (!batch.empty() && bytes + j->est_bytes > lane_budget) break;
+                if (!batch.empty() && (bytes + j->est_bytes > lane_budget ||
+                                       (cfg.max_batch_voxels && vox + j->voxels > cfg.max_batch_voxels)))
+                    break;
                 bytes += j->est_bytes;
+                vox += j->voxels;
                 batch.push_back(j);
                 pending.pop_front();
             }
@@ -129,6 +133,7 @@ QSES_API void qses_server_config_default(qses_server_config *c) {
     c->lanes = 2;
     c->memory_budget = 120ull << 30;
     c->max_batch = 256;
+    c->max_batch_voxels = 1000000000ull;
 }
 
 QSES_API int qses_server_create(const qses_server_config *cfg, qses_server **out) {
@@ -182,6 +187,7 @@ QSES_API int qses_server_submit(qses_server *s, const qses_request *req, unsigne
         int rc = qses::grid_from_bounds(mn, mx, maxR, req->n, req->voxel, g, &gi, nullptr);
         if (rc != QSES_OK) return rc;  // rejected at admission, never queued
         j->est_bytes = estimate_bytes(g, req->n);
+        j->voxels = (unsigned long long)g.G * g.G * g.G;
         if (j->est_bytes > s->cfg.memory_budget) return QSES_ERR_OUT_OF_MEMORY;
     }
     std::lock_guard<std::mutex> lock(s->mu);
