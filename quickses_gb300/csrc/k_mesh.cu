@@ -651,17 +651,12 @@ __device__ __forceinline__ void prefetch_l2(const void *p) {
 __device__ __forceinline__ void prefetch_l1(const void *p) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
-// Weak loads either way: the CTA- and GPU-scope acquires of the dataflow order them.
-template <unsigned kFlags>
-__device__ __forceinline__ float4 gs_load_pos(const float4 *pos4, unsigned id) {
-    return (kFlags & kGsL1Positions) ? pos4[id] : __ldcg(pos4 + id);
-}
 
 // Warp roles: warp 0 takes boundary arrivals from lower slabs, warp 1 sends this slab's
 // cross-slab releases (GPU-scope atomics, off the workers' critical path), the other warps
 // update vertices.
 template <int kGsT, unsigned kFlags>
-__global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned S,
+__global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned S,
                                                   const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
                                                   const unsigned short *__restrict__ cnt_local, int *remote,
                                                   unsigned *inbox, unsigned *inbox_tail, int *err,
@@ -794,57 +789,28 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                 __nanosleep(20);
                 continue;
             }
-            // Chain state: the last vertex this warp updated and its new position (every lane
-            // holds it), and the inputs prefetched for the vertex it expects to update next.
-            unsigned prev = 0xffffffffu, pf_v = 0xffffffffu, pf_id = 0u;
-            float px = 0.0f, py = 0.0f, pz = 0.0f;
-            float4 pf_q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             while (v != 0xffffffffu) {  // follow the chain of vertices this warp releases
                 __threadfence_block();
                 const long long c0 = clock64();
-                const unsigned e0 = st[v - a], e1 = st[v - a + 1], deg = e1 - e0;
+                const unsigned e0 = st[v - a], e1 = st[v - a + 1];
                 float sx = 0.0f, sy = 0.0f, sz = 0.0f;
                 unsigned first_id = v;
-                unsigned w = 0xffffffffu, wid = 0u;  // the next vertex of the chain and its ids
-                if ((kFlags & kGsChain) && deg <= 32u) {
-                    unsigned id;
-                    float4 q;
-                    if (pf_v == v) {  // inputs loaded while the previous vertex ran
-                        id = pf_id;
-                        q = pf_q;
-                    } else {
-                        id = lane < deg ? __ldg(nbr + e0 + lane) : v;
-                        q = gs_load_pos<kFlags>(pos4, id);
-                    }
-                    first_id = id;
-                    // A local higher neighbour whose pending lower entries are exactly v's: every
-                    // other input of it is final now, so its inputs can be fetched while v runs.
-                    const bool hl = lane < deg && id > v && id < b;
-                    const unsigned grp = __match_any_sync(0xffffffffu, hl ? id : 0xffffffffu);
-                    bool ok = false;
-                    if (hl && (unsigned)(__ffs(grp) - 1) == lane) {
-                        const unsigned o = id - a;
-                        const unsigned c = (((volatile unsigned *)cnt)[o >> 1] >> (16u * (o & 1u))) & 0xffffu;
-                        ok = c == (unsigned)__popc(grp) && st[o + 1] - st[o] <= 32u;
-                    }
-                    const unsigned cm = __ballot_sync(0xffffffffu, ok);
-                    if (cm) {
-                        w = __shfl_sync(0xffffffffu, id, __ffs(cm) - 1);
-                        __threadfence_block();  // acquire: the counter value seen above is final
-                        const unsigned we = st[w - a], wd = st[w - a + 1] - we;
-                        wid = lane < wd ? __ldg(nbr + we + lane) : w;
-                    }
-                    // The previous chain vertex's store may not be visible to a load issued
-                    // before it; its value is in registers.
-                    if (prev != 0xffffffffu && id == prev) q = make_float4(px, py, pz, 0.0f);
-                    const float qx = lane < deg ? q.x : 0.0f, qy = lane < deg ? q.y : 0.0f, qz = lane < deg ? q.z : 0.0f;
+                for (unsigned base = e0; base < e1; base += 32) {
+                    const unsigned m = min(32u, e1 - base);
+                    const unsigned id = lane < m ? __ldg(nbr + base + lane) : v;
+                    if (base == e0) first_id = id;
+                    // Weak loads either way: the CTA- and GPU-scope acquires above order them.
+                    const float4 q = (kFlags & kGsL1Positions) ? pos4[id] : __ldcg(pos4 + id);
+                    // strictly in neighbour-list order; lanes past m add +0.0f (a sum that
+                    // started at +0.0f is unchanged by it)
+                    const float qx = lane < m ? q.x : 0.0f, qy = lane < m ? q.y : 0.0f, qz = lane < m ? q.z : 0.0f;
 #pragma unroll
                     for (unsigned k = 0; k < 16; k++) {
                         sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
                         sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
                         sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
                     }
-                    if (deg > 16) {
+                    if (m > 16) {
 #pragma unroll
                         for (unsigned k = 16; k < 32; k++) {
                             sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
@@ -852,42 +818,14 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                             sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
                         }
                     }
-                } else {
-                    for (unsigned base = e0; base < e1; base += 32) {
-                        const unsigned m = min(32u, e1 - base);
-                        const unsigned id = lane < m ? __ldg(nbr + base + lane) : v;
-                        if (base == e0) first_id = id;
-                        const float4 q = gs_load_pos<kFlags>(pos4, id);
-                        // strictly in neighbour-list order; lanes past m add +0.0f (a sum that
-                        // started at +0.0f is unchanged by it)
-                        const float qx = lane < m ? q.x : 0.0f, qy = lane < m ? q.y : 0.0f, qz = lane < m ? q.z : 0.0f;
-#pragma unroll
-                        for (unsigned k = 0; k < 16; k++) {
-                            sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
-                            sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
-                            sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
-                        }
-                        if (m > 16) {
-#pragma unroll
-                            for (unsigned k = 16; k < 32; k++) {
-                                sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
-                                sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
-                                sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
-                            }
-                        }
-                    }
                 }
-                // Every lane holds the same sums (each added the broadcast values in order).
-                const float n = (float)(int)deg;
-                const float nx = __fdiv_rn(sx, n), ny = __fdiv_rn(sy, n), nz = __fdiv_rn(sz, n);
+                const float n = (float)(int)(e1 - e0);
                 if (lane == 0) {
-                    __stcg(pos4 + v, make_float4(nx, ny, nz, 0.0f));
+                    __stcg(pos4 + v, make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f));
                     // Successors in this slab read the new position after a CTA-scope
                     // acquire; successors in higher slabs get it through the sender warp.
                     __threadfence_block();
                 }
-                float4 wq = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                if (w != 0xffffffffu) wq = gs_load_pos<kFlags>(pos4, wid);  // overlaps v's release
                 const long long c1 = clock64();
                 __syncwarp();
                 // Release: one lane per neighbour entry.
@@ -919,28 +857,15 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                         }
                     }
                     unsigned mask = __ballot_sync(0xffffffffu, ready);
-                    const unsigned wm = __ballot_sync(0xffffffffu, ready && u == w);
                     if (mask && next == 0xffffffffu) {
-                        // continue with the prefetched vertex when it is ready, else the first
-                        const unsigned f = wm ? (unsigned)(__ffs(wm) - 1) : (unsigned)(__ffs(mask) - 1);
-                        next = __shfl_sync(0xffffffffu, u, f);
+                        const unsigned f = __ffs(mask) - 1;
+                        next = __shfl_sync(0xffffffffu, u, f);  // continue with it directly
                         mask &= ~(1u << f);
                     }
                     if ((mask >> lane) & 1u) ring_push16(ring, &s_tail, u - a);
                 }
                 __syncwarp();  // queued releases precede the done count the sender checks
                 if (lane == 0) atomicAdd(&s_done, 1u);
-                prev = v;
-                px = nx;
-                py = ny;
-                pz = nz;
-                if (w != 0xffffffffu && next == w) {
-                    pf_v = w;
-                    pf_id = wid;
-                    pf_q = wq;
-                } else {
-                    pf_v = 0xffffffffu;
-                }
                 v = next;
                 const long long c2 = clock64();
                 cyc_update += c1 - c0;
@@ -1066,13 +991,12 @@ void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s
     k_from_float4<<<nblk(nv, 256), 256, 0, s>>>(v4, nv, v3);
 }
 static const void *gs_flow_fn(int threads, unsigned flags) {
-#define QSES_GS_FNS(T)                                                                                  \
-    {(const void *)k_gs_flow<T, 0>, (const void *)k_gs_flow<T, 1>, (const void *)k_gs_flow<T, 2>,       \
-     (const void *)k_gs_flow<T, 3>, (const void *)k_gs_flow<T, 4>, (const void *)k_gs_flow<T, 5>,       \
-     (const void *)k_gs_flow<T, 6>, (const void *)k_gs_flow<T, 7>}
-    static const void *fn[2][8] = {QSES_GS_FNS(512), QSES_GS_FNS(1024)};
-#undef QSES_GS_FNS
-    return fn[threads >= 1024 ? 1 : 0][flags & 7u];
+    static const void *fn[2][4] = {
+        {(const void *)k_gs_flow<512, 0>, (const void *)k_gs_flow<512, 1>, (const void *)k_gs_flow<512, 2>,
+         (const void *)k_gs_flow<512, 3>},
+        {(const void *)k_gs_flow<1024, 0>, (const void *)k_gs_flow<1024, 1>, (const void *)k_gs_flow<1024, 2>,
+         (const void *)k_gs_flow<1024, 3>}};
+    return fn[threads >= 1024 ? 1 : 0][flags & 3u];
 }
 cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads, unsigned flags,
                            const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,

@@ -53,13 +53,11 @@ int gs_slab_max_blocks(int device, unsigned S, int threads);
 struct GsShape {
     int threads = 512;
     unsigned target = 16384;
-    unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions | kGsChain
+    unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions
 };
 // Cache policies of the smoothing kernel (same results, different memory paths):
 constexpr unsigned kGsL1Prefetch = 1;   // prefetch a successor's neighbour list into L1, not L2
 constexpr unsigned kGsL1Positions = 2;  // neighbour positions through L1 (default: L2 only)
-constexpr unsigned kGsChain = 4;        // fetch the inputs of the vertex a warp updates next
-                                        // while it updates the current one
 // Tuned shape for a mesh of nv vertices (batch = waves of many molecules), or the default.
 GsShape gs_shape(unsigned nv, bool batch);
 void gs_shape_record(unsigned nv, bool batch, GsShape s);

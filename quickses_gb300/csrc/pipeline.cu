@@ -135,12 +135,11 @@ void gs_shape_record(unsigned nv, bool batch, GsShape sh) {
 }
 
 int gs_shape_candidates(GsShape *out, int max) {
-    static const unsigned targets[] = {4096, 16384, 25000};
-    static const unsigned flags[] = {0, 2, kGsChain, kGsChain | 2, kGsChain | 3};
+    static const unsigned targets[] = {4096, 8192, 16384, 25000};
     int k = 0;
     for (int t : {512, 1024})
         for (unsigned tg : targets)
-            for (unsigned f : flags)
+            for (unsigned f = 0; f < 4; f++)
                 if (k < max) out[k++] = GsShape{t, tg, f};
     return k;
 }
