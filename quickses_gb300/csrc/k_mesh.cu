@@ -656,7 +656,7 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // cross-slab releases (GPU-scope atomics, off the workers' critical path), the other warps
 // update vertices.
 template <int kGsT, unsigned kFlags>
-__global__ void __launch_bounds__(kGsT) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned S,
+__global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned S,
                                                   const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
                                                   const unsigned short *__restrict__ cnt_local, int *remote,
                                                   unsigned *inbox, unsigned *inbox_tail, int *err,
