@@ -174,8 +174,9 @@ QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_f
                            float *smooth_ms_out);
 /* Fixes the smoothing launch shape of ctx: threads 512 or 1024 per slab CTA, slab size
  * aimed at (>= 256 vertices), cache_flags bit 0 = prefetch successors' neighbour lists into
- * L1 instead of L2, bit 1 = neighbour positions through L1; threads = 0 returns to the
- * tuned/default shape.  Every shape gives the same mesh. */
+ * L1 instead of L2, bit 1 = neighbour positions through L1, bit 2 = keep the positions in
+ * persisting L2 lines during the pass (a window on the context's stream, cleared after it);
+ * threads = 0 returns to the tuned/default shape.  Every shape gives the same mesh. */
 QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags);
 /* The same for the batch form, timing whole qses_compute_batch calls on `reqs`. */
 QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, unsigned count, int repeats,

@@ -439,7 +439,7 @@ QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned t
         ctx->gs_force = qses::GsShape{0, 0, 0};
         return QSES_OK;
     }
-    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 3) return QSES_ERR_INVALID_ARG;
+    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 7) return QSES_ERR_INVALID_ARG;
     ctx->gs_force = qses::GsShape{threads, target, cache_flags};
     return QSES_OK;
 }

@@ -14,6 +14,7 @@
 //                 updated once every lower-id neighbour has been, exactly as the sequential
 //                 loop would see them.
 #include <cfloat>
+#include <cstring>
 
 #include "device_common.cuh"
 #include "kernels.h"
@@ -1009,6 +1010,30 @@ cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, in
                     &inbox_tail, &err, &spin_cycles, &stats};
     return cudaLaunchCooperativeKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
 }
+void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes) {
+    int max_persist = 0, max_window = 0;
+    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, device);
+    cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, device);
+    cudaStreamAttrValue attr;
+    memset(&attr, 0, sizeof(attr));
+    if (bytes > 0 && max_persist > 0 && max_window > 0) {
+        const size_t window = bytes < (size_t)max_window ? bytes : (size_t)max_window;
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)max_persist);
+        attr.accessPolicyWindow.base_ptr = const_cast<void *>(p);
+        attr.accessPolicyWindow.num_bytes = window;
+        attr.accessPolicyWindow.hitRatio = window <= (size_t)max_persist ? 1.0f : (float)max_persist / (float)window;
+        attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &attr);
+    } else {
+        attr.accessPolicyWindow.num_bytes = 0;
+        cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &attr);
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
+    cudaGetLastError();  // the window is a hint: a refusal leaves the results unchanged
+}
+
 int gs_slab_max_blocks(int device, unsigned S, int threads) {
     const void *fn = gs_flow_fn(threads, 0);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);

@@ -53,11 +53,15 @@ int gs_slab_max_blocks(int device, unsigned S, int threads);
 struct GsShape {
     int threads = 512;
     unsigned target = 16384;
-    unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions
+    unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions | kGsPersistL2
 };
 // Cache policies of the smoothing kernel (same results, different memory paths):
 constexpr unsigned kGsL1Prefetch = 1;   // prefetch a successor's neighbour list into L1, not L2
 constexpr unsigned kGsL1Positions = 2;  // neighbour positions through L1 (default: L2 only)
+constexpr unsigned kGsPersistL2 = 4;    // host side: keep the positions in persisting L2 lines
+// Sets (bytes > 0) or clears the stream's L2 persistence window over [p, p + bytes); the
+// set-aside is this process's context limit, restored when the window is cleared.
+void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes);
 // Tuned shape for a mesh of nv vertices (batch = waves of many molecules), or the default.
 GsShape gs_shape(unsigned nv, bool batch);
 void gs_shape_record(unsigned nv, bool batch, GsShape s);

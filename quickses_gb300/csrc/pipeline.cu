@@ -135,11 +135,12 @@ void gs_shape_record(unsigned nv, bool batch, GsShape sh) {
 }
 
 int gs_shape_candidates(GsShape *out, int max) {
-    static const unsigned targets[] = {4096, 8192, 16384, 25000};
+    static const unsigned targets[] = {4096, 16384, 25000};
+    static const unsigned flags[] = {0, kGsL1Positions, kGsPersistL2, kGsPersistL2 | kGsL1Positions};
     int k = 0;
     for (int t : {512, 1024})
         for (unsigned tg : targets)
-            for (unsigned f = 0; f < 4; f++)
+            for (unsigned f : flags)
                 if (k < max) out[k++] = GsShape{t, tg, f};
     return k;
 }
@@ -380,6 +381,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         if (P <= pmax) {
             launch_to_float4(vq, nv, pos4, s);
             ctx->launches++;
+            if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, pos4, 16ull * nv);
             for (int pass = 0; pass < p.smooth_passes; pass++) {
                 launch_gs_setup(deg, nbr, 0, nv, S, (unsigned short *)cnt, lower, s);
                 ctx->launches++;
@@ -393,6 +395,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
                 ctx->diag[1] = S;
                 ctx->launches++;
             }
+            if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, nullptr, 0);
             launch_from_float4(pos4, nv, vq, s);
             ctx->launches++;
         } else {

@@ -328,6 +328,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         if (fits) {
             launch_to_float4(vq, nv, pos4, s);
             ctx->launches++;
+            if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, pos4, 16ull * nv);
             for (int pass = 0; pass < passes; pass++) {
                 for (auto &w : waves) {
                     const unsigned nw = w.second - w.first;
@@ -348,6 +349,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
                     ctx->diag[0] = std::max<unsigned long long>(ctx->diag[0], (unsigned long long)P);
                 }
             }
+            if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, nullptr, 0);
             launch_from_float4(pos4, nv, vq, s);
             ctx->launches++;
         } else {

@@ -54,7 +54,8 @@ def test_smoothing_at_scale_exact(big):
     assert np.array_equal(m1.triangles, m0.triangles)
 
 
-@pytest.mark.parametrize("threads,target,flags", [(1024, 16384, 0), (1024, 4096, 3), (512, 25000, 2)])
+@pytest.mark.parametrize("threads,target,flags", [(1024, 16384, 0), (1024, 4096, 3), (512, 25000, 2),
+                                                  (1024, 16384, 4), (1024, 16384, 6)])
 def test_smoothing_shapes_at_scale_exact(big, threads, target, flags):
     """~150 slabs, every cache policy: still the sequential Gauss-Seidel result."""
     xyz, rad, _, m0, _, _, _ = big
