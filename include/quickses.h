@@ -231,8 +231,9 @@ QSES_API int qses_stage_times(qses_context *ctx, float *ms, const char **names, 
 QSES_API int qses_last_launch_count(qses_context *ctx);
 /* Smoothing diagnostics of the last call: [0] slabs, [1] vertices per slab, [2] most
  * boundary polls of one slab, [3] slabs that did not finish, [4] clock cycles spent in
- * vertex updates, [5] in releasing successors, [6] vertices updated (summed over threads).
- * Returns the number of values written. */
+ * vertex updates, [5] in releasing successors, [6] vertices updated, [7] cycles until a
+ * vertex's neighbour ids arrived, [8] then until their positions arrived (summed over
+ * warps).  Returns the number of values written. */
 QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max);
 
 /* ------------------------------------------------------- allocation-free field */

@@ -216,10 +216,10 @@ class Context:
         return int(self._lib.qses_last_launch_count(self._h))
 
     def diagnostics(self):
-        out = (ctypes.c_ulonglong * 8)()
-        k = self._lib.qses_diagnostics(self._h, out, 8)
+        out = (ctypes.c_ulonglong * 10)()
+        k = self._lib.qses_diagnostics(self._h, out, 10)
         names = ["slabs", "slab_size", "max_polls", "unfinished_slabs", "update_cycles", "release_cycles",
-                 "vertices"]
+                 "vertices", "id_wait_cycles", "position_wait_cycles"]
         return {names[q]: int(out[q]) for q in range(min(k, len(names)))}
 
 

@@ -558,7 +558,7 @@ QSES_API int qses_last_launch_count(qses_context *ctx) { return ctx ? ctx->launc
 QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max) {
     if (!ctx || !out) return 0;
     int k = 0;
-    for (; k < max && k < 8; k++) out[k] = ctx->diag[k];
+    for (; k < max && k < 10; k++) out[k] = ctx->diag[k];
     return k;
 }
 

@@ -230,8 +230,10 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
                                          const unsigned *__restrict__ outMask, unsigned char *__restrict__ codes,
                                          unsigned *__restrict__ signMask) {
     __shared__ unsigned s_out[kEdtH * kEdtH][3];
-    __shared__ unsigned char s_g[kEdtH * kEdtH][32];
-    __shared__ unsigned char s_h[kEdtH][kEdtTY][32];
+    // Squared distances, one byte per voxel (255 = none); the y and x passes work on four
+    // voxels per 32-bit word with saturating byte adds, so 255 stays "none".
+    __shared__ __align__(16) unsigned char s_g[kEdtH * kEdtH][32];
+    __shared__ __align__(16) unsigned char s_h[kEdtH][kEdtTY][32];
     __shared__ unsigned s_in[kEdtTX * kEdtTY], s_ot[kEdtTX * kEdtTY];
     const int j0 = jb * kEdtTY, i0 = ib * kEdtTX;
     const int R = g.R, G = g.G, W = g.W, t = threadIdx.x;
@@ -270,7 +272,7 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
         has_out = __syncthreads_or(any);
     }
     if (has_border && has_out) {
-        // z: distance (in voxels, <= R) to the nearest outside voxel along the row.
+        // z: squared distance (in voxels, <= R^2) to the nearest outside voxel along the row.
         for (int q = t; q < HX * HY * 32; q += kEdtNT) {
             const int row = q >> 5, b = q & 31;
             const unsigned a = s_out[row][0], c = s_out[row][1], d = s_out[row][2];
@@ -281,20 +283,20 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
                 unsigned long long dn = (((unsigned long long)c << 32) | a) << (31 - b);
                 int dd = dn ? __clzll((long long)dn) : 1000;
                 int m = min(du, dd);
-                if (m <= R) gv = (unsigned char)m;
+                if (m <= R) gv = (unsigned char)(m * m);
             }
             s_g[row][b] = gv;
         }
         __syncthreads();
-        // y: min over dj of dj^2 + g^2.
-        for (int q = t; q < HX * kEdtTY * 32; q += kEdtNT) {
-            const int b = q & 31, y = (q >> 5) % kEdtTY, hx = (q >> 5) / kEdtTY;
-            int best = 255;
+        // y: min over dj of dj^2 + g^2 (<= 2 R^2 = 162 < 255), four voxels per word.
+        for (int q = t; q < HX * kEdtTY * 8; q += kEdtNT) {
+            const int w4 = q & 7, y = (q >> 3) % kEdtTY, hx = (q >> 3) / kEdtTY;
+            unsigned best = 0xffffffffu;
             for (int dj = -R; dj <= R; dj++) {
-                int gv = s_g[hx * HY + y + R + dj][b];
-                if (gv != 255) best = min(best, dj * dj + gv * gv);
+                const unsigned gw = reinterpret_cast<const unsigned *>(s_g[hx * HY + y + R + dj])[w4];
+                best = __vminu4(best, __vaddus4(gw, (unsigned)(dj * dj) * 0x01010101u));
             }
-            s_h[hx][y][b] = (unsigned char)best;
+            reinterpret_cast<unsigned *>(s_h[hx][y])[w4] = best;
         }
         __syncthreads();
     }
@@ -303,6 +305,16 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
     unsigned sgn = 0u;
     if (i < G && j < G) {
         const unsigned iw = s_in[row], ow = s_ot[row];
+        // min over di of di^2 + h (<= 3 R^2 = 243 < 255) for this thread's 8 voxels
+        unsigned bw0 = 0xffffffffu, bw1 = 0xffffffffu;
+        if (has_out) {
+            for (int di = -R; di <= R; di++) {
+                const unsigned *hrow = reinterpret_cast<const unsigned *>(s_h[x + R + di][y]);
+                const unsigned d2 = (unsigned)(di * di) * 0x01010101u;
+                bw0 = __vminu4(bw0, __vaddus4(hrow[2 * part], d2));
+                bw1 = __vminu4(bw1, __vaddus4(hrow[2 * part + 1], d2));
+            }
+        }
         unsigned long long packed = 0ull;
 #pragma unroll
         for (int e = 0; e < 8; e++) {
@@ -313,15 +325,8 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
             else if (ow & bit) code = QSES_CODE_OUT;
             else if (iw & bit) code = QSES_CODE_IN;
             else {
-                code = QSES_CODE_NONE;
-                if (has_out) {
-                    int best = 255;
-                    for (int di = -R; di <= R; di++) {
-                        int hv = s_h[x + R + di][y][b];
-                        if (hv != 255) best = min(best, di * di + hv);
-                    }
-                    if (best != 255) code = (unsigned)best;
-                }
+                const unsigned best = ((e < 4 ? bw0 : bw1) >> (8 * (e & 3))) & 0xffu;
+                code = best != 255u ? best : QSES_CODE_NONE;
             }
             packed |= (unsigned long long)code << (8 * e);
             if ((valid & bit) && code != QSES_CODE_OUT && (int)code >= g.negmin) sgn |= bit;

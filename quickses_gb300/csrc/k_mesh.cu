@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
     __syncthreads();
 
     const unsigned lane = threadIdx.x & 31;
-    unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0;
+    unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0, cyc_ids = 0, cyc_pos = 0;
     if (threadIdx.x < 32) {
         // Warp 0 only takes boundary arrivals (the last lower-slab dependency of a vertex
         // finished); it never updates vertices, so arrivals are never stuck behind a chain.
@@ -800,8 +800,18 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                     const unsigned m = min(32u, e1 - base);
                     const unsigned id = lane < m ? __ldg(nbr + base + lane) : v;
                     if (base == e0) first_id = id;
+                    long long ca = 0;
+                    if (stats && base == e0) {  // diagnostics: when the ids have arrived
+                        asm volatile("" ::"r"(id));
+                        ca = clock64();
+                        cyc_ids += ca - c0;
+                    }
                     // Weak loads either way: the CTA- and GPU-scope acquires above order them.
                     const float4 q = (kFlags & kGsL1Positions) ? pos4[id] : __ldcg(pos4 + id);
+                    if (stats && base == e0) {  // ... and their positions
+                        asm volatile("" ::"f"(q.x));
+                        cyc_pos += clock64() - ca;
+                    }
                     // strictly in neighbour-list order; lanes past m add +0.0f (a sum that
                     // started at +0.0f is unchanged by it)
                     const float qx = lane < m ? q.x : 0.0f, qy = lane < m ? q.y : 0.0f, qz = lane < m ? q.z : 0.0f;
@@ -885,6 +895,8 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
             atomicAdd(stats + 2, cyc_update);
             atomicAdd(stats + 3, cyc_release);
             atomicAdd(stats + 4, nproc);
+            atomicAdd(stats + 5, cyc_ids);
+            atomicAdd(stats + 6, cyc_pos);
         }
     }
 }

@@ -431,7 +431,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     QCHK(cudaMemcpyAsync(ctx->h_small + 2048, (char *)ctx->small + 256, 64, cudaMemcpyDeviceToHost, s));
     QCHK(cudaStreamSynchronize(s));
     ctx->mark("filter");
-    memcpy(ctx->diag + 2, ctx->h_small + 2048, 5 * sizeof(unsigned long long));
+    memcpy(ctx->diag + 2, ctx->h_small + 2048, 7 * sizeof(unsigned long long));
     if (!keep_all && T > 0) {
         memcpy(&tot, ctx->h_small, sizeof(tot));
         nkept = tot.x;
