@@ -243,7 +243,8 @@ def run_gpu(args):
                    "l2": "flushed between timed steps (256 MB write outside the event pair)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "smoothing_shape": None if tuned is None else
-                   {"threads": tuned[0], "slab_target": tuned[1], "cache_flags": tuned[2]}},
+                   {"threads": tuned[0], "slab_target": tuned[1], "cache_flags": tuned[2]},
+                   "refine_tile": None if tuned is None else ("16x8" if tuned[3] == 1 else "8x8")},
         "e2e": {"value": e2e_value, "unit": "voxels/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "qses_compute (C-ABI, pageable host atoms in, pinned host mesh out)"},

@@ -165,13 +165,16 @@ QSES_API void qses_set_pinned_cache(unsigned long long bytes);
 /* ------------------------------------------------------------------ autotuner */
 
 /* Picks the smoothing launch shape (threads per slab CTA, slab size aimed at) for meshes of
- * this size by running the molecule once per candidate shape (`repeats` times each) and
- * keeping the fastest; later calls of this process on meshes of the same size class (log2
+ * this size, and the refine tile shape for grids of this size, by running the molecule once
+ * per candidate shape (`repeats` times each) and keeping the fastest; later calls of this process on meshes of the same size class (log2
  * of the vertex count) use it.  The mesh is identical for every shape: the update order is
  * fixed by the vertex ids.  No reference counterpart (QuickSES hard-codes its launches). */
 QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_float3 *atoms, const float *radii,
                            unsigned n, int repeats, int *threads_out, unsigned *target_out, unsigned *flags_out,
-                           float *smooth_ms_out);
+                           int *field_shape_out, float *smooth_ms_out);
+/* Fixes the refine tile shape of ctx: 0 = 8 x 8 z-rows per CTA, 1 = 16 x 8 (less halo per
+ * row, more shared memory); -1 returns to the tuned/default shape.  Same codes for both. */
+QSES_API int qses_set_field_shape(qses_context *ctx, int shape);
 /* Fixes the smoothing launch shape of ctx: threads 512 or 1024 per slab CTA, slab size
  * aimed at (>= 256 vertices), cache_flags bit 0 = prefetch successors' neighbour lists into
  * L1 instead of L2, bit 1 = neighbour positions through L1, bit 2 = keep the positions in

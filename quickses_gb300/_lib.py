@@ -86,7 +86,8 @@ SIGNATURES = {
     "qses_set_smoothing_shape": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint, ctypes.c_uint]),
     "qses_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _FP, ctypes.c_uint, ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),
-                                     ctypes.POINTER(ctypes.c_uint), _FP]),
+                                     ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_int), _FP]),
+    "qses_set_field_shape": (ctypes.c_int, [_VP, ctypes.c_int]),
     "qses_autotune_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),
                                            ctypes.POINTER(ctypes.c_uint), _FP]),

@@ -160,16 +160,22 @@ class Context:
                     "qses_set_smoothing_shape")
 
     def autotune(self, xyz, radii, voxel=0.5, smooth=1, repeats=1):
-        """Times every smoothing launch shape on this molecule and keeps the fastest for its
-        mesh size class; returns (threads, slab target, smoothing ms)."""
+        """Times every smoothing launch shape and refine tile shape on this molecule and keeps
+        the fastest for its size class; returns (threads, slab target, cache flags, refine
+        tile shape, smoothing ms)."""
         xyz, radii = _f32(xyz, 3), _f32(radii)
-        th, tg, fl, ms = ctypes.c_int(0), ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_float(0)
+        th, tg, fl, fs, ms = ctypes.c_int(0), ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_int(0), ctypes.c_float(0)
         rc = self._lib.qses_autotune(self._h, ctypes.byref(self._params(voxel, smooth, False, 300)),
                                      xyz.ctypes.data_as(ctypes.c_void_p),
                                      radii.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), xyz.shape[0], int(repeats),
-                                     ctypes.byref(th), ctypes.byref(tg), ctypes.byref(fl), ctypes.byref(ms))
+                                     ctypes.byref(th), ctypes.byref(tg), ctypes.byref(fl), ctypes.byref(fs),
+                                     ctypes.byref(ms))
         self._check(rc, "qses_autotune")
-        return th.value, tg.value, fl.value, ms.value
+        return th.value, tg.value, fl.value, fs.value, ms.value
+
+    def set_field_shape(self, shape=-1):
+        """Fix the refine tile shape (0: 8 x 8 rows, 1: 16 x 8); -1 = tuned/default."""
+        self._check(self._lib.qses_set_field_shape(self._h, int(shape)), "qses_set_field_shape")
 
     def autotune_batch(self, requests, repeats=1):
         arrays, reqs = _requests(requests)

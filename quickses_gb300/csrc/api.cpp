@@ -444,9 +444,15 @@ QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned t
     return QSES_OK;
 }
 
+QSES_API int qses_set_field_shape(qses_context *ctx, int shape) {
+    if (!ctx || shape < -1 || shape >= qses::kEdtShapes) return QSES_ERR_INVALID_ARG;
+    ctx->edt_force = shape;
+    return QSES_OK;
+}
+
 QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_float3 *atoms, const float *radii,
                            unsigned n, int repeats, int *threads_out, unsigned *target_out, unsigned *flags_out,
-                           float *smooth_ms_out) {
+                           int *field_shape_out, float *smooth_ms_out) {
     if (!ctx || !p || (n && (!atoms || !radii))) return QSES_ERR_INVALID_ARG;
     int rc = check_params(ctx, p);
     if (rc) return rc;
@@ -486,8 +492,42 @@ QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_f
         }
     }
     ctx->gs_force = qses::GsShape{0, 0, 0};
+    // refine tile shape, timed on the same molecule (the codes are the same for every shape)
+    int best_edt = 0;
+    float best_edt_ms = -1.0f;
+    if (n > 1 && rc == QSES_OK) {
+        for (int sh = 0; sh < qses::kEdtShapes && rc == QSES_OK; sh++) {
+            ctx->edt_force = sh;
+            for (int r = 0; r < std::max(1, repeats) && rc == QSES_OK; r++) {
+                if (ctx->input.reserve(16ull * n + 512) != QSES_OK) {
+                    rc = ctx->fail(QSES_ERR_OUT_OF_MEMORY, "input buffers");
+                    break;
+                }
+                float *d_xyz = (float *)ctx->input.take(12ull * n);
+                float *d_r = (float *)ctx->input.take(4ull * n);
+                cudaError_t e = cudaMemcpyAsync(d_xyz, atoms, 12ull * n, cudaMemcpyHostToDevice, ctx->stream);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(d_r, radii, 4ull * n, cudaMemcpyHostToDevice, ctx->stream);
+                if (e != cudaSuccess) {
+                    rc = ctx->fail(QSES_ERR_CUDA, "atom upload", e);
+                    break;
+                }
+                qses_params p0 = *p;
+                p0.smooth_passes = 0;
+                rc = qses::run_pipeline(ctx, p0, d_xyz, d_r, n);
+                if (rc) break;
+                for (auto &t : ctx->times)
+                    if (!strcmp(t.first, "refine") && (best_edt_ms < 0 || t.second < best_edt_ms)) {
+                        best_edt_ms = t.second;
+                        best_edt = sh;
+                    }
+            }
+        }
+        ctx->edt_force = -1;
+        if (rc == QSES_OK && ctx->have_grid) qses::edt_shape_record(ctx->grid.G, best_edt);
+    }
     ctx->profiling = prof;
     if (rc) return rc;
+    if (field_shape_out) *field_shape_out = best_edt;
     if (nv > 0) qses::gs_shape_record(nv, false, best);
     if (threads_out) *threads_out = best.threads;
     if (target_out) *target_out = best.target;

@@ -223,35 +223,40 @@ __global__ void __launch_bounds__(kSasNT) k_sas(QGrid g, const float4 *__restric
 
 // ------------------------------------------------------------------ refine
 
-constexpr int kEdtTX = 8, kEdtTY = 8, kEdtNT = 256, kEdtH = kEdtTX + 2 * QSES_RMAX;
+constexpr int kEdtNT = 256;
 
-// One refine tile: z-word w of the 8 x 8 rows starting at (8 ib, 8 jb), with an R halo.
+// One refine tile: z-word w of the TX x TY rows starting at (TX ib, TY jb), with an R halo.
+// Larger tiles re-read less halo per row (the z pass runs on (TX+2R)(TY+2R) rows for TX TY
+// output rows) at the cost of shared memory; the shape is chosen by the autotuner.
+
+template <int TX, int TY>
 __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, const unsigned *__restrict__ inMask,
                                          const unsigned *__restrict__ outMask, unsigned char *__restrict__ codes,
                                          unsigned *__restrict__ signMask) {
-    __shared__ unsigned s_out[kEdtH * kEdtH][3];
+    constexpr int HXM = TX + 2 * QSES_RMAX, HYM = TY + 2 * QSES_RMAX;
+    __shared__ unsigned s_out[HXM * HYM][3];
     // Squared distances, one byte per voxel (255 = none); the y and x passes work on four
     // voxels per 32-bit word with saturating byte adds, so 255 stays "none".
-    __shared__ __align__(16) unsigned char s_g[kEdtH * kEdtH][32];
-    __shared__ __align__(16) unsigned char s_h[kEdtH][kEdtTY][32];
-    __shared__ unsigned s_in[kEdtTX * kEdtTY], s_ot[kEdtTX * kEdtTY];
-    const int j0 = jb * kEdtTY, i0 = ib * kEdtTX;
+    __shared__ __align__(16) unsigned char s_g[HXM * HYM][32];
+    __shared__ __align__(16) unsigned char s_h[HXM][TY][32];
+    __shared__ unsigned s_in[TX * TY], s_ot[TX * TY];
+    const int j0 = jb * TY, i0 = ib * TX;
     const int R = g.R, G = g.G, W = g.W, t = threadIdx.x;
-    const int HX = kEdtTX + 2 * R, HY = kEdtTY + 2 * R, k0 = w * 32;
+    const int HX = TX + 2 * R, HY = TY + 2 * R, k0 = w * 32;
     const unsigned valid = (k0 + 32 <= G) ? 0xffffffffu : ((1u << (G - k0)) - 1u);
 
     int anyb = 0;
-    if (t < kEdtTX * kEdtTY) {
-        int i = i0 + t / kEdtTY, j = j0 + t % kEdtTY;
+    for (int q = t; q < TX * TY; q += kEdtNT) {
+        int i = i0 + q / TY, j = j0 + q % TY;
         unsigned iw = 0u, ow = 0xffffffffu;
         if (i < G && j < G) {
             size_t idx = ((size_t)i * G + j) * W + w;
             iw = inMask[idx];
             ow = outMask[idx];
-            anyb = (valid & ~iw & ~ow) != 0u;
+            anyb |= (valid & ~iw & ~ow) != 0u;
         }
-        s_in[t] = iw;
-        s_ot[t] = ow;
+        s_in[q] = iw;
+        s_ot[q] = ow;
     }
     const int has_border = __syncthreads_or(anyb);
     int has_out = 0;
@@ -289,8 +294,8 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
         }
         __syncthreads();
         // y: min over dj of dj^2 + g^2 (<= 2 R^2 = 162 < 255), four voxels per word.
-        for (int q = t; q < HX * kEdtTY * 8; q += kEdtNT) {
-            const int w4 = q & 7, y = (q >> 3) % kEdtTY, hx = (q >> 3) / kEdtTY;
+        for (int q = t; q < HX * TY * 8; q += kEdtNT) {
+            const int w4 = q & 7, y = (q >> 3) % TY, hx = (q >> 3) / TY;
             unsigned best = 0xffffffffu;
             for (int dj = -R; dj <= R; dj++) {
                 const unsigned gw = reinterpret_cast<const unsigned *>(s_g[hx * HY + y + R + dj])[w4];
@@ -300,8 +305,10 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
         }
         __syncthreads();
     }
-    // x: min over di of di^2 + h, then codes and sign bits; 4 threads per row, 8 voxels each.
-    const int row = t >> 2, part = t & 3, x = row / kEdtTY, y = row % kEdtTY, i = i0 + x, j = j0 + y;
+    // x: min over di of di^2 + h, then codes and sign bits; 4 threads per row, 8 voxels each
+    // (TX TY / 64 rows per thread: the same trip count in every warp).
+    for (int row = t >> 2; row < TX * TY; row += kEdtNT / 4) {
+    const int part = t & 3, x = row / TY, y = row % TY, i = i0 + x, j = j0 + y;
     unsigned sgn = 0u;
     if (i < G && j < G) {
         const unsigned iw = s_in[row], ow = s_ot[row];
@@ -336,12 +343,14 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
     sgn |= __shfl_xor_sync(0xffffffffu, sgn, 1);
     sgn |= __shfl_xor_sync(0xffffffffu, sgn, 2);
     if (part == 0 && i < G && j < G) signMask[((size_t)i * G + j) * W + w] = sgn;
+    }
 }
 
+template <int TX, int TY>
 __global__ void __launch_bounds__(kEdtNT) k_edt(QGrid g, const unsigned *__restrict__ inMask,
                                                 const unsigned *__restrict__ outMask,
                                                 unsigned char *__restrict__ codes, unsigned *__restrict__ signMask) {
-    edt_tile(g, blockIdx.x, blockIdx.y, blockIdx.z, inMask, outMask, codes, signMask);
+    edt_tile<TX, TY>(g, blockIdx.x, blockIdx.y, blockIdx.z, inMask, outMask, codes, signMask);
 }
 
 // ------------------------------------------------------------ batched field
@@ -386,8 +395,8 @@ __global__ void __launch_bounds__(kEdtNT) k_edt_batch(QBatch b, const unsigned *
     int w, jb, ib;
     while (next_tile(b, counter, m, w, jb, ib)) {
         const QMol mol = b.mols[m];
-        edt_tile(mol.g, w, jb, ib, inMask + mol.mask_off, outMask + mol.mask_off, codes + mol.code_off,
-                 signMask + mol.mask_off);
+        edt_tile<8, 8>(mol.g, w, jb, ib, inMask + mol.mask_off, outMask + mol.mask_off, codes + mol.code_off,
+                       signMask + mol.mask_off);
     }
 }
 
@@ -409,9 +418,12 @@ void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigne
     k_sas<<<grid, kSasNT, 0, s>>>(g, atoms, cells, inMask, outMask);
 }
 void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
-                unsigned *signMask, cudaStream_t s) {
-    dim3 grid(g.W, (g.G + kEdtTY - 1) / kEdtTY, (g.G + kEdtTX - 1) / kEdtTX);
-    k_edt<<<grid, kEdtNT, 0, s>>>(g, inMask, outMask, codes, signMask);
+                unsigned *signMask, cudaStream_t s, int shape) {
+    // shape 0: 8 x 8 rows (37 KB of shared memory), 1: 16 x 8 rows (48 KB, the static limit)
+    const int TX = shape >= 1 ? 16 : 8, TY = 8;
+    dim3 grid(g.W, (g.G + TY - 1) / TY, (g.G + TX - 1) / TX);
+    if (shape >= 1) k_edt<16, 8><<<grid, kEdtNT, 0, s>>>(g, inMask, outMask, codes, signMask);
+    else k_edt<8, 8><<<grid, kEdtNT, 0, s>>>(g, inMask, outMask, codes, signMask);
 }
 static unsigned persistent_blocks(const void *fn, int threads, unsigned items) {
     int dev = 0, sms = 0, per_sm = 0;

@@ -237,7 +237,7 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
 }
 
 template <bool EMIT, bool FULL>
-__global__ void __launch_bounds__(256) k_mc(QGrid g, const unsigned *__restrict__ sign,
+__global__ void __launch_bounds__(256, 3) k_mc(QGrid g, const unsigned *__restrict__ sign,
                                             const unsigned char *__restrict__ codes, const float *__restrict__ lut,
                                             uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
                                             unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey) {

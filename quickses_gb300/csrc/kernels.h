@@ -13,8 +13,9 @@ void launch_atom_gather(const float *xyz, const float *r, const unsigned *skey, 
                         float4 *atoms, uint2 *cells, cudaStream_t s);
 void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigned *inMask, unsigned *outMask,
                 cudaStream_t s);
+// shape: refine tile of 8 x 8 (0) or 16 x 8 (1) z-rows; the same codes for both.
 void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
-                unsigned *signMask, cudaStream_t s);
+                unsigned *signMask, cudaStream_t s, int shape = 0);
 
 void launch_mc_count(const QGrid &g, const unsigned *sign, uint2 *rowCount, cudaStream_t s);
 void launch_mc_emit(const QGrid &g, const unsigned *sign, const unsigned char *codes, const float *lut,
@@ -66,6 +67,10 @@ void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes);
 GsShape gs_shape(unsigned nv, bool batch);
 void gs_shape_record(unsigned nv, bool batch, GsShape s);
 int gs_shape_candidates(GsShape *out, int max);
+// Tuned refine tile shape (launch_edt `shape`) for grids of G voxels per axis, or 0.
+int edt_shape(int G);
+void edt_shape_record(int G, int shape);
+constexpr int kEdtShapes = 2;
 constexpr unsigned kGsSlabMaxVerts = 25000;
 
 // ---- batch forms (QBatch: per-molecule grids and offsets in device memory)

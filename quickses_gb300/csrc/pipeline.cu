@@ -134,6 +134,21 @@ void gs_shape_record(unsigned nv, bool batch, GsShape sh) {
     g_tuned[batch][b] = true;
 }
 
+static int g_edt_tune[2][16];  // [tuned?][log2 G]
+
+int edt_shape(int G) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const int b = std::min(bits_for((unsigned)G), 15);
+    return g_edt_tune[0][b] ? g_edt_tune[1][b] : 0;
+}
+
+void edt_shape_record(int G, int shape) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const int b = std::min(bits_for((unsigned)G), 15);
+    g_edt_tune[0][b] = 1;
+    g_edt_tune[1][b] = shape;
+}
+
 int gs_shape_candidates(GsShape *out, int max) {
     static const unsigned targets[] = {4096, 16384, 25000};
     static const unsigned flags[] = {0, kGsL1Positions, kGsPersistL2, kGsPersistL2 | kGsL1Positions};
@@ -266,7 +281,8 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     launch_sas(g, atoms, cells, inMask, outMask, s);
     ctx->launches++;
     ctx->mark("sas");
-    launch_edt(g, inMask, outMask, codes, signMask, s);
+    ctx->edt_used = ctx->edt_force >= 0 ? ctx->edt_force : edt_shape(g.G);
+    launch_edt(g, inMask, outMask, codes, signMask, s, ctx->edt_used);
     ctx->launches++;
     ctx->mark("refine");
 

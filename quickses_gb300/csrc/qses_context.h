@@ -78,6 +78,8 @@ struct qses_context {
     int launches = 0;
     qses::GsShape gs_force{0, 0, 0};  // autotuner: forced smoothing shape (threads 0 = none)
     qses::GsShape gs_used;            // shape of the last smoothing run
+    int edt_force = -1;               // autotuner: forced refine tile shape (-1 = none)
+    int edt_used = 0;
     unsigned long long diag[10] = {0};  // smoothing diagnostics: slabs, slab size, max/idle/total rounds
 
     int fail(int code, const char *what, cudaError_t e = cudaSuccess);

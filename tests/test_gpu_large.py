@@ -31,6 +31,15 @@ def big():
     return xyz, rad, g, m0, codes, m1, m1k
 
 
+def test_field_16x8_tiles_match(big):
+    """The 16 x 8 refine tile gives the same 664^3 codes as the 8 x 8 one."""
+    xyz, rad, g, _, codes, _, _ = big
+    with q.Context(0) as c:
+        c.set_field_shape(1)
+        c.compute(xyz, rad, voxel=WL.voxel, smooth=0)
+        assert np.array_equal(c.debug_codes(g.G), codes)
+
+
 @pytest.mark.parametrize("x0", [0, 200, 330, 640])
 def test_field_slab_exact(big, x0):
     xyz, rad, g, _, codes, _, _ = big

@@ -63,6 +63,20 @@ def test_field_codes_exact(ctx, kind, n, seed, dx):
         mism[:5].tolist(), codes[tuple(mism[:5].T)].tolist(), ref[tuple(mism[:5].T)].tolist())
 
 
+@pytest.mark.parametrize("shape", [0, 1])
+@pytest.mark.parametrize("kind,n,seed,dx", CASES[1:])
+def test_field_codes_every_tile_shape(ctx, kind, n, seed, dx, shape):
+    """Both refine tile shapes (8 x 8 and 16 x 8 z-rows per CTA) give the oracle's codes."""
+    xyz, rad = _atoms(kind, n, seed)
+    ctx.set_field_shape(shape)
+    try:
+        ctx.compute(xyz, rad, voxel=dx, smooth=0)
+    finally:
+        ctx.set_field_shape(-1)
+    g, _ = O.grid(xyz, rad, dx)
+    assert np.array_equal(ctx.debug_codes(g.G), O.field_codes(xyz, rad, g, fp64=False))
+
+
 @pytest.mark.parametrize("kind,n,seed,dx", CASES)
 def test_atom_order_exact(ctx, kind, n, seed, dx):
     """Cell keys equal the oracle's except at exact cell boundaries (where the reference's
