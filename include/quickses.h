@@ -179,8 +179,11 @@ QSES_API int qses_set_field_shape(qses_context *ctx, int shape);
  * aimed at (>= 256 vertices), cache_flags bit 0 = prefetch successors' neighbour lists into
  * L1 instead of L2, bit 1 = neighbour positions through L1, bit 2 = keep the positions in
  * persisting L2 lines during the pass (a window on the context's stream, cleared after it);
- * threads = 0 returns to the tuned/default shape.  Every shape gives the same mesh. */
-QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags);
+ * wave_vertices = most vertices per slab-kernel launch (0 = as many as fit: 152 SMs x 25 000;
+ * larger meshes run as sequential waves); threads = 0 returns to the tuned/default shape.
+ * Every shape gives the same mesh. */
+QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags,
+                                      unsigned wave_vertices);
 /* The same for the batch form, timing whole qses_compute_batch calls on `reqs`. */
 QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, unsigned count, int repeats,
                                  int *threads_out, unsigned *target_out, unsigned *flags_out, float *ms_out);

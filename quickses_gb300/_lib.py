@@ -83,7 +83,7 @@ SIGNATURES = {
     "qses_compute_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.POINTER(Mesh),
                                           ctypes.POINTER(ctypes.c_int)]),
     "qses_set_pinned_cache": (None, [ctypes.c_ulonglong]),
-    "qses_set_smoothing_shape": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint, ctypes.c_uint]),
+    "qses_set_smoothing_shape": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]),
     "qses_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _FP, ctypes.c_uint, ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),
                                      ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_int), _FP]),

@@ -153,11 +153,11 @@ class Context:
                 self._lib.qses_mesh_release(ctypes.byref(meshes[i]))
         return out
 
-    def set_smoothing_shape(self, threads=0, target=16384, cache_flags=0):
-        """Fix the smoothing launch shape (threads 512/1024, slab target, cache flags);
-        threads 0 = tuned/default."""
-        self._check(self._lib.qses_set_smoothing_shape(self._h, int(threads), int(target), int(cache_flags)),
-                    "qses_set_smoothing_shape")
+    def set_smoothing_shape(self, threads=0, target=16384, cache_flags=0, wave_vertices=0):
+        """Fix the smoothing launch shape (threads 512/1024, slab target, cache flags, most
+        vertices per slab-kernel wave); threads 0 = tuned/default."""
+        self._check(self._lib.qses_set_smoothing_shape(self._h, int(threads), int(target), int(cache_flags),
+                                                       int(wave_vertices)), "qses_set_smoothing_shape")
 
     def autotune(self, xyz, radii, voxel=0.5, smooth=1, repeats=1):
         """Times every smoothing launch shape and refine tile shape on this molecule and keeps

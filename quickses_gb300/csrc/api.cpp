@@ -227,8 +227,6 @@ QSES_API int qses_context_create(int device, void *cuda_stream, qses_context **o
         qses_context_destroy(ctx);
         return QSES_ERR_OUT_OF_MEMORY;
     }
-    int maxb = qses::gs_max_blocks(device);
-    ctx->gs_blocks = maxb < 16 ? maxb : 16;
     *out = ctx;
     return QSES_OK;
 }
@@ -433,14 +431,17 @@ QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, uns
 
 QSES_API void qses_set_pinned_cache(unsigned long long bytes) { pinned_pool().set_cap((size_t)bytes); }
 
-QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags) {
+QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags,
+                                      unsigned wave_vertices) {
     if (!ctx) return QSES_ERR_INVALID_ARG;
     if (threads == 0) {
-        ctx->gs_force = qses::GsShape{0, 0, 0};
+        ctx->gs_force = qses::GsShape{0, 0, 0, 0};
         return QSES_OK;
     }
-    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 7) return QSES_ERR_INVALID_ARG;
-    ctx->gs_force = qses::GsShape{threads, target, cache_flags};
+    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 7 ||
+        (wave_vertices != 0 && wave_vertices < target))
+        return QSES_ERR_INVALID_ARG;
+    ctx->gs_force = qses::GsShape{threads, target, cache_flags, wave_vertices};
     return QSES_OK;
 }
 
@@ -491,7 +492,7 @@ QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_f
             }
         }
     }
-    ctx->gs_force = qses::GsShape{0, 0, 0};
+    ctx->gs_force = qses::GsShape{0, 0, 0, 0};
     // refine tile shape, timed on the same molecule (the codes are the same for every shape)
     int best_edt = 0;
     float best_edt_ms = -1.0f;
@@ -563,7 +564,7 @@ QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, un
             }
         }
     }
-    ctx->gs_force = qses::GsShape{0, 0, 0};
+    ctx->gs_force = qses::GsShape{0, 0, 0, 0};
     if (rc) return rc;
     if (nv > 0) qses::gs_shape_record((unsigned)std::min<unsigned long long>(nv, 152ull * qses::kGsSlabMaxVerts), true, best);
     if (threads_out) *threads_out = best.threads;

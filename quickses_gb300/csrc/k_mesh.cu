@@ -9,7 +9,7 @@
 //  k_weld_*       unique quantised positions in lexicographic order (CudaSurf.cu:444-457)
 //  k_closest      closest atom per welded vertex (closestAtomPerVertex, Kernels.cu:547-604)
 //  k_tri_*        drop triangles with a repeated index (CudaSurf.cu:820-829)
-//  k_csr_* / k_gs neighbour lists in triangle order and the in-place Gauss-Seidel Laplacian
+//  k_csr_* / k_gs_flow  neighbour lists in triangle order and the in-place Gauss-Seidel Laplacian
 //                 in vertex-id order (SmoothMesh.cpp:45-123), run as a dataflow: a vertex is
 //                 updated once every lower-id neighbour has been, exactly as the sequential
 //                 loop would see them.
@@ -495,91 +495,24 @@ __global__ void k_csr_fill(const unsigned *__restrict__ tri, const unsigned *__r
     nbr[2 * p + 1] = c == 2 ? b : d;
 }
 
-__global__ void k_lower_count(const uint2 *__restrict__ start, const unsigned *__restrict__ nbr, unsigned nv,
-                              int *__restrict__ lower) {
-    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nv) return;
-    const unsigned e1 = v + 1 < nv ? start[v + 1].x : start[nv].x;
-    int c = 0;
-    for (unsigned e = start[v].x; e < e1; e++) c += nbr[e] < v;
-    lower[v] = c;
-}
-
-__global__ void k_gs_seed(const int *__restrict__ lower, int *__restrict__ cnt, unsigned nv,
-                          unsigned *__restrict__ queue, unsigned *__restrict__ qtail) {
-    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nv) return;
-    const int c = lower[v];
-    cnt[v] = c;
-    if (c == 0) queue[atomicAdd(qtail, 1u)] = v;
-}
-
-// One Gauss-Seidel pass.  Threads take queue slots in order; a slot is filled when its
-// vertex's last lower neighbour finishes, so every vertex reads final values for lower ids
-// and untouched values for higher ids, in its own neighbour-list order.  All waits are
-// bounded by `spin_cycles`.
-__global__ void __launch_bounds__(256) k_gs(float *pos, unsigned nv, const uint2 *__restrict__ start,
-                                            const unsigned *__restrict__ nbr, int *cnt, unsigned *queue,
-                                            unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles) {
-    for (;;) {
-        const unsigned idx = atomicAdd(qhead, 1u);
-        if (idx >= nv) return;
-        unsigned v = 0xffffffffu;
-        const long long t0 = clock64();
-        for (unsigned it = 0;; it++) {
-            v = ld_acquire_u32(&queue[idx]);
-            if (v != 0xffffffffu) break;
-            if ((it & 63u) == 63u && clock64() - t0 > spin_cycles) {
-                raise_error(err, QSES_ERR_TIMEOUT);
-                return;
-            }
-            __nanosleep(100);
-        }
-        if (v >= nv) {
-            raise_error(err, QSES_ERR_INTERNAL);
-            return;
-        }
-        const unsigned e0 = start[v].x, e1 = v + 1 < nv ? start[v + 1].x : start[nv].x;
-        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-        for (unsigned e = e0; e < e1; e++) {
-            const unsigned u = nbr[e];
-            sx = __fadd_rn(sx, __ldcg(pos + 3ull * u));
-            sy = __fadd_rn(sy, __ldcg(pos + 3ull * u + 1));
-            sz = __fadd_rn(sz, __ldcg(pos + 3ull * u + 2));
-        }
-        const float n = (float)(int)(e1 - e0);
-        __stcg(pos + 3ull * v, __fdiv_rn(sx, n));
-        __stcg(pos + 3ull * v + 1, __fdiv_rn(sy, n));
-        __stcg(pos + 3ull * v + 2, __fdiv_rn(sz, n));
-        __threadfence();
-        for (unsigned e = e0; e < e1; e++) {
-            const unsigned u = nbr[e];
-            if (u > v && atomicSub(&cnt[u], 1) == 1) {
-                __threadfence();
-                const unsigned slot = atomicAdd(qtail, 1u);
-                if (slot < nv) st_release_u32(&queue[slot], u);
-            }
-        }
-    }
-}
-
-// Slab-partitioned Gauss-Seidel pass.  Vertex ids are split into P contiguous slabs, one
-// persistent CTA each.  Every dependency edge goes from a lower to a higher id, so a chain
-// of updates crosses each slab boundary at most once: readiness inside a slab is tracked
-// with shared-memory counters and processed in rounds separated by __syncthreads, and only
-// boundary edges go through global memory (an acquire/release counter per vertex and a
-// per-slab inbox).  Each vertex is still computed exactly as the sequential loop would.
-constexpr int kGsSlabMaxSmem = 200 * 1024;  // dynamic part: ring + packed counters, 6 B/vertex
-
 __device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
     int old;
     asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(-v) : "memory");
     return old;
 }
 
+// Slab-partitioned Gauss-Seidel pass.  Vertex ids are split into P contiguous slabs, one
+// persistent CTA each.  Every dependency edge goes from a lower to a higher id, so a chain
+// of updates crosses each slab boundary at most once: readiness inside a slab is tracked
+// with shared-memory counters and a ring of ready vertices, and only boundary edges go
+// through global memory (an acquire/release counter per vertex and a per-slab inbox).
+// Each vertex is still computed exactly as the sequential loop would.
+constexpr int kGsSlabMaxSmem = 200 * 1024;  // dynamic part: offsets, packed counters, ring: 8 B/vertex
+
 // Per vertex: lower-id neighbour entries inside its slab (+1 if any lie in lower slabs),
 // and the count of entries in lower slabs.
-// Vertices [v0, v1) form the slabs; no neighbour of theirs lies outside that range.
+// Vertices [v0, v1) form the slabs.  Neighbours below v0 belong to waves that finished
+// before this one (final values); neighbours at or above v1 are read before their update.
 __global__ void k_gs_setup(const uint2 *__restrict__ start, const unsigned *__restrict__ nbr, unsigned v0,
                            unsigned v1, unsigned S, unsigned short *__restrict__ cnt_local, int *__restrict__ remote) {
     unsigned v = v0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -588,7 +521,7 @@ __global__ void k_gs_setup(const uint2 *__restrict__ start, const unsigned *__re
     unsigned loc = 0, rem = 0;
     for (unsigned e = start[v].x; e < start[v + 1].x; e++) {
         const unsigned u = nbr[e];
-        if (u < v) {
+        if (u < v && u >= v0) {  // below v0: an earlier wave, already final
             if (u >= lo) loc++; else rem++;
         }
     }
@@ -981,17 +914,6 @@ void launch_copy_keys(const unsigned *tri, size_t n3, unsigned *keys, cudaStream
 void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s) {
     k_csr_fill<<<nblk(n3, 256), 256, 0, s>>>(tri, socc, n3, nbr);
 }
-void launch_lower_count(const uint2 *start, const unsigned *nbr, unsigned nv, int *lower, cudaStream_t s) {
-    k_lower_count<<<nblk(nv, 256), 256, 0, s>>>(start, nbr, nv, lower);
-}
-void launch_gs_seed(const int *lower, int *cnt, unsigned nv, unsigned *queue, unsigned *qtail, cudaStream_t s) {
-    k_gs_seed<<<nblk(nv, 256), 256, 0, s>>>(lower, cnt, nv, queue, qtail);
-}
-cudaError_t launch_gs(float *pos, unsigned nv, const uint2 *start, const unsigned *nbr, int *cnt, unsigned *queue,
-                      unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles, int blocks, cudaStream_t s) {
-    void *args[] = {&pos, &nv, (void *)&start, (void *)&nbr, &cnt, &queue, &qhead, &qtail, &err, &spin_cycles};
-    return cudaLaunchCooperativeKernel((const void *)k_gs, dim3(blocks), dim3(256), args, 0, s);
-}
 void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, unsigned S,
                      unsigned short *cnt_local, int *remote, cudaStream_t s) {
     k_gs_setup<<<nblk(v1 - v0, 256), 256, 0, s>>>(start, nbr, v0, v1, S, cnt_local, remote);
@@ -1051,12 +973,6 @@ int gs_slab_max_blocks(int device, unsigned S, int threads) {
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
     int per_sm = 0, sms = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads >= 1024 ? 1024 : 512, gs_slab_smem(S));
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    return per_sm * sms;
-}
-int gs_max_blocks(int device) {
-    int per_sm = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gs, 256, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     return per_sm * sms;
 }

@@ -31,11 +31,6 @@ void launch_tri_compact(const unsigned *tri, unsigned nt, const uint2 *excl, uns
 void launch_degree(const unsigned *tri, size_t n3, unsigned nv, uint2 *deg, cudaStream_t s);
 void launch_copy_keys(const unsigned *tri, size_t n3, unsigned *keys, cudaStream_t s);
 void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s);
-void launch_lower_count(const uint2 *start, const unsigned *nbr, unsigned nv, int *lower, cudaStream_t s);
-void launch_gs_seed(const int *lower, int *cnt, unsigned nv, unsigned *queue, unsigned *qtail, cudaStream_t s);
-cudaError_t launch_gs(float *pos, unsigned nv, const uint2 *start, const unsigned *nbr, int *cnt, unsigned *queue,
-                      unsigned *qhead, unsigned *qtail, int *err, long long spin_cycles, int blocks, cudaStream_t s);
-int gs_max_blocks(int device);
 void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, unsigned S,
                      unsigned short *cnt_local, int *remote, cudaStream_t s);
 size_t gs_slab_smem(unsigned S);
@@ -55,6 +50,7 @@ struct GsShape {
     int threads = 512;
     unsigned target = 16384;
     unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions | kGsPersistL2
+    unsigned wave = 0;   // most vertices per slab-kernel launch (0: all that fit on the GPU)
 };
 // Cache policies of the smoothing kernel (same results, different memory paths):
 constexpr unsigned kGsL1Prefetch = 1;   // prefetch a successor's neighbour list into L1, not L2

@@ -201,6 +201,49 @@ void Arena::release() {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+int run_smoothing(qses_context *ctx, const GsShape &sh, int passes, float *vq, float4 *pos4, unsigned nv,
+                  const uint2 *deg, const unsigned *nbr, unsigned short *cnt, int *remote, unsigned *inbox,
+                  unsigned *inbox_tail, int *d_err, unsigned long long *stats, bool record_slabs) {
+    cudaStream_t s = ctx->stream;
+    const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts, sh.threads), 1024);
+    if (pmax < 1) return ctx->fail(QSES_ERR_NO_DEVICE, "the smoothing kernel does not fit on this device");
+    unsigned long long cap = (unsigned long long)pmax * kGsSlabMaxVerts;
+    if (sh.wave && sh.wave < cap) cap = sh.wave;
+    const unsigned nwaves = (unsigned)((nv + cap - 1) / cap);
+    const unsigned wsize = (nv + nwaves - 1) / nwaves;  // balanced waves
+    launch_to_float4(vq, nv, pos4, s);
+    ctx->launches++;
+    if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, pos4, 16ull * nv);
+    if (stats) QCHK(cudaMemsetAsync(stats, 0, 64, s));
+    for (int pass = 0; pass < passes; pass++) {
+        for (unsigned v0 = 0; v0 < nv; v0 += wsize) {
+            const unsigned v1 = std::min(nv, v0 + wsize), nw = v1 - v0;
+            int P = (int)std::min<unsigned>((nw + sh.target - 1) / sh.target, (unsigned)pmax);
+            if (P < 1) P = 1;
+            unsigned S = (nw + P - 1) / P;
+            if (S > kGsSlabMaxVerts) {
+                P = (int)((nw + kGsSlabMaxVerts - 1) / kGsSlabMaxVerts);
+                S = (nw + P - 1) / P;
+            }
+            launch_gs_setup(deg, nbr, v0, v1, S, cnt, remote, s);
+            ctx->launches++;
+            QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * P * S, s));
+            QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
+            QCHK(launch_gs_slab(pos4, v0, v1, S, P, sh.threads, sh.flags, deg, nbr, cnt, remote, inbox, inbox_tail,
+                                d_err, 4000000000ll, stats, s));
+            ctx->launches++;
+            if (record_slabs) {
+                ctx->diag[0] = std::max<unsigned long long>(ctx->diag[0], (unsigned long long)P);
+                ctx->diag[1] = std::max<unsigned long long>(ctx->diag[1], (unsigned long long)S);
+            }
+        }
+    }
+    if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, nullptr, 0);
+    launch_from_float4(pos4, nv, vq, s);
+    ctx->launches++;
+    return QSES_OK;
+}
+
 int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n) {
     cudaStream_t s = ctx->stream;
     ctx->launches = 0;
@@ -329,7 +372,6 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     unsigned *oval = (unsigned *)B.take(4 * n3 + 4), *oval2 = (unsigned *)B.take(4 * n3 + 4);
     unsigned *nbr = (unsigned *)B.take(8 * n3 + 8);
     int *lower = (int *)B.take(4ull * NE + 4), *cnt = (int *)B.take(4ull * NE + 4);
-    unsigned *queue = (unsigned *)B.take(4ull * NE + 4);
     unsigned *inbox = (unsigned *)B.take(4ull * NE + 4096);
     unsigned *inbox_tail = (unsigned *)B.take(4096);
     float4 *pos4 = (float4 *)B.take(16ull * NE + 16);
@@ -383,52 +425,12 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         launch_csr_fill(tri, socc, n3, nbr, s);
         ctx->launches++;
         ctx->mark("smooth_csr");
-        // Slab-partitioned exact Gauss-Seidel: P persistent CTAs, contiguous id slabs of S.
         const GsShape sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(nv, false);
         ctx->gs_used = sh;
-        const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts, sh.threads), 1024);
-        int P = (int)std::min<unsigned>((nv + sh.target - 1) / sh.target, (unsigned)pmax);
-        if (P < 1) P = 1;
-        unsigned S = (nv + P - 1) / P;
-        if (S > kGsSlabMaxVerts) {
-            P = (int)((nv + kGsSlabMaxVerts - 1) / kGsSlabMaxVerts);
-            S = (nv + P - 1) / P;
-        }
-        if (P <= pmax) {
-            launch_to_float4(vq, nv, pos4, s);
-            ctx->launches++;
-            if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, pos4, 16ull * nv);
-            for (int pass = 0; pass < p.smooth_passes; pass++) {
-                launch_gs_setup(deg, nbr, 0, nv, S, (unsigned short *)cnt, lower, s);
-                ctx->launches++;
-                QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * P * S, s));
-                QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
-                unsigned long long *stats = (unsigned long long *)((char *)ctx->small + 256);
-                QCHK(cudaMemsetAsync(stats, 0, 64, s));
-                QCHK(launch_gs_slab(pos4, 0, nv, S, P, sh.threads, sh.flags, deg, nbr, (unsigned short *)cnt, lower, inbox,
-                                    inbox_tail, d_err, 4000000000ll, stats, s));
-                ctx->diag[0] = P;
-                ctx->diag[1] = S;
-                ctx->launches++;
-            }
-            if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, nullptr, 0);
-            launch_from_float4(pos4, nv, vq, s);
-            ctx->launches++;
-        } else {
-            // Very large meshes: global-memory dataflow (same arithmetic, slower hand-offs).
-            launch_lower_count(deg, nbr, nv, lower, s);
-            ctx->launches++;
-            unsigned *qctl = (unsigned *)((char *)ctx->small + 128);
-            int blocks = std::min(ctx->gs_blocks, 64);
-            for (int pass = 0; pass < p.smooth_passes; pass++) {
-                QCHK(cudaMemsetAsync(queue, 0xff, 4ull * nv, s));
-                QCHK(cudaMemsetAsync(qctl, 0, 8, s));
-                launch_gs_seed(lower, cnt, nv, queue, qctl + 1, s);
-                ctx->launches++;
-                QCHK(launch_gs(vq, nv, deg, nbr, cnt, queue, qctl, qctl + 1, d_err, 4000000000ll, blocks, s));
-                ctx->launches++;
-            }
-        }
+        unsigned long long *stats = (unsigned long long *)((char *)ctx->small + 256);
+        int rc2 = run_smoothing(ctx, sh, p.smooth_passes, vq, pos4, nv, deg, nbr, (unsigned short *)cnt, lower, inbox,
+                                inbox_tail, d_err, stats, true);
+        if (rc2) return rc2;
     }
     ctx->mark("smooth");
 

@@ -248,7 +248,6 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     unsigned *oval = (unsigned *)B.take(4 * n3 + 4), *oval2 = (unsigned *)B.take(4 * n3 + 4);
     unsigned *nbr = (unsigned *)B.take(8 * n3 + 8);
     int *lower = (int *)B.take(4ull * NE + 4), *cnt = (int *)B.take(4ull * NE + 4);
-    unsigned *queue = (unsigned *)B.take(4ull * NE + 4);
     unsigned *inbox = (unsigned *)B.take(4ull * NE + 65536);
     unsigned *inbox_tail = (unsigned *)B.take(4096);
     float4 *pos4 = (float4 *)B.take(16ull * NE + 16);
@@ -308,65 +307,12 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         launch_csr_fill(tri, socc, n3, nbr, s);
         ctx->launches++;
         ctx->mark("smooth_csr");
-        // Waves of whole molecules, each at most pmax slabs of kGsSlabMaxVerts vertices.
-        const GsShape sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(std::min<unsigned>(nv, 152u * kGsSlabMaxVerts), true);
+        const GsShape sh = ctx->gs_force.threads ? ctx->gs_force
+                                                  : gs_shape(std::min<unsigned>(nv, 152u * kGsSlabMaxVerts), true);
         ctx->gs_used = sh;
-        const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts, sh.threads), 1024);
-        const unsigned long long cap = (unsigned long long)pmax * kGsSlabMaxVerts;
-        std::vector<std::pair<unsigned, unsigned>> waves;
-        bool fits = pmax > 0;
-        for (unsigned m = 0; m < nm && fits;) {
-            const unsigned v0 = vtx_off[m];
-            unsigned e = m;
-            while (e < nm && (unsigned long long)vtx_off[e + 1] - v0 <= cap) e++;
-            if (e == m) fits = false;  // one molecule alone exceeds a wave
-            else {
-                if (vtx_off[e] > v0) waves.push_back({v0, vtx_off[e]});
-                m = e;
-            }
-        }
-        if (fits) {
-            launch_to_float4(vq, nv, pos4, s);
-            ctx->launches++;
-            if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, pos4, 16ull * nv);
-            for (int pass = 0; pass < passes; pass++) {
-                for (auto &w : waves) {
-                    const unsigned nw = w.second - w.first;
-                    int P = (int)std::min<unsigned>((nw + sh.target - 1) / sh.target, (unsigned)pmax);
-                    if (P < 1) P = 1;
-                    unsigned S = (nw + P - 1) / P;
-                    if (S > kGsSlabMaxVerts) {
-                        P = (int)((nw + kGsSlabMaxVerts - 1) / kGsSlabMaxVerts);
-                        S = (nw + P - 1) / P;
-                    }
-                    launch_gs_setup(deg, nbr, w.first, w.second, S, (unsigned short *)cnt, lower, s);
-                    ctx->launches++;
-                    QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * P * S, s));
-                    QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
-                    QCHK(launch_gs_slab(pos4, w.first, w.second, S, P, sh.threads, sh.flags, deg, nbr, (unsigned short *)cnt,
-                                        lower, inbox, inbox_tail, d_err, 4000000000ll, nullptr, s));
-                    ctx->launches++;
-                    ctx->diag[0] = std::max<unsigned long long>(ctx->diag[0], (unsigned long long)P);
-                }
-            }
-            if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, nullptr, 0);
-            launch_from_float4(pos4, nv, vq, s);
-            ctx->launches++;
-        } else {
-            launch_lower_count(deg, nbr, nv, lower, s);
-            ctx->launches++;
-            unsigned *qctl = (unsigned *)((char *)ctx->small + 128);
-            const int blocks = std::min(ctx->gs_blocks, 64);
-            for (int pass = 0; pass < passes; pass++) {
-                QCHK(cudaMemsetAsync(queue, 0xff, 4ull * nv, s));
-                QCHK(cudaMemsetAsync(qctl, 0, 8, s));
-                launch_gs_seed(lower, cnt, nv, queue, qctl + 1, s);
-                ctx->launches++;
-                QCHK(launch_gs(vq, nv, deg, nbr, cnt, queue, qctl, qctl + 1, d_err, 4000000000ll, blocks, s));
-                ctx->launches++;
-            }
-        }
-        ctx->diag[1] = waves.size();
+        int rc2 = run_smoothing(ctx, sh, passes, vq, pos4, nv, deg, nbr, (unsigned short *)cnt, lower, inbox,
+                                inbox_tail, d_err, nullptr, true);
+        if (rc2) return rc2;
     }
     ctx->mark("smooth");
 

@@ -63,7 +63,6 @@ struct qses_context {
     qses::Arena input, field, mesh_ws;
     void *small = nullptr;            // 4 KB device scratch: bounds, error word, queue counters
     unsigned char *h_small = nullptr; // 4 KB pinned host scratch
-    int gs_blocks = 16;
     QGrid grid;
     qses_grid_info info;
     bool have_grid = false;
@@ -76,7 +75,7 @@ struct qses_context {
     std::vector<std::pair<const char *, cudaEvent_t>> marks;
     std::vector<std::pair<const char *, float>> times;
     int launches = 0;
-    qses::GsShape gs_force{0, 0, 0};  // autotuner: forced smoothing shape (threads 0 = none)
+    qses::GsShape gs_force{0, 0, 0, 0};  // autotuner: forced smoothing shape (threads 0 = none)
     qses::GsShape gs_used;            // shape of the last smoothing run
     int edt_force = -1;               // autotuner: forced refine tile shape (-1 = none)
     int edt_used = 0;
@@ -88,6 +87,13 @@ struct qses_context {
 
 namespace qses {
 int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n);
+// `passes` exact Gauss-Seidel passes over vertices [0, nv): positions vq (3 floats each) in
+// and out, CSR (deg offsets, nbr), shape sh.  The vertices run in sequential waves of at
+// most the slab kernel's capacity; every dependency points to a lower id, so a wave only
+// depends on earlier, finished waves.
+int run_smoothing(qses_context *ctx, const GsShape &sh, int passes, float *vq, float4 *pos4, unsigned nv,
+                  const uint2 *deg, const unsigned *nbr, unsigned short *cnt, int *remote, unsigned *inbox,
+                  unsigned *inbox_tail, int *d_err, unsigned long long *stats, bool record_slabs);
 // All items share `passes`; the weld keys of every item fit `key_bits` bits and
 // key_bits + bits(count - 1) <= 64.  Results in ctx->batch.
 int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int passes, int key_bits);

@@ -77,6 +77,21 @@ def test_uneven_batch_matches_single(ctx):
         _same(m, _single(ctx, r))
 
 
+def test_small_waves_match_single(ctx):
+    """Sequential smoothing waves that cut through molecules give the same meshes."""
+    reqs = [_req(*q.molecules.ball(n, 500 + n)[:2], 0.4, 2) for n in (900, 4000, 12000, 2500)]
+    singles = [_single(ctx, r) for r in reqs]
+    ctx.set_smoothing_shape(1024, 4096, 0, 50000)
+    try:
+        out = ctx.compute_batch(reqs)
+        one = _single(ctx, reqs[2])
+    finally:
+        ctx.set_smoothing_shape(0)
+    for m, s1 in zip(out, singles):
+        _same(m, s1)
+    _same(one, singles[2])
+
+
 def test_multi_wave_smoothing_matches_single(ctx):
     """More vertices than one Gauss-Seidel wave holds (152 slabs x 25 000), so the batch
     is smoothed in several waves."""

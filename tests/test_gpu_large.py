@@ -63,14 +63,16 @@ def test_smoothing_at_scale_exact(big):
     assert np.array_equal(m1.triangles, m0.triangles)
 
 
-@pytest.mark.parametrize("threads,target,flags", [(1024, 16384, 0), (1024, 4096, 3), (512, 25000, 2),
-                                                  (1024, 16384, 4), (1024, 16384, 6)])
-def test_smoothing_shapes_at_scale_exact(big, threads, target, flags):
-    """~150 slabs, every cache policy: still the sequential Gauss-Seidel result."""
+@pytest.mark.parametrize("threads,target,flags,wave", [(1024, 16384, 0, 0), (1024, 4096, 3, 0), (512, 25000, 2, 0),
+                                                       (1024, 16384, 4, 0), (1024, 16384, 6, 0),
+                                                       (1024, 16384, 0, 1000000), (512, 8192, 2, 600000)])
+def test_smoothing_shapes_at_scale_exact(big, threads, target, flags, wave):
+    """~150 slabs, every cache policy, and the mesh split into sequential waves (as meshes
+    above 3.8 M vertices are): still the sequential Gauss-Seidel result."""
     xyz, rad, _, m0, _, _, _ = big
     ref = O.smooth_f32(m0.vertices, m0.triangles, 1)
     with q.Context(0) as c:
-        c.set_smoothing_shape(threads, target, flags)
+        c.set_smoothing_shape(threads, target, flags, wave)
         m = c.compute(xyz, rad, voxel=WL.voxel, smooth=1, keep_degenerate=True)
     assert np.array_equal(m.vertices, ref)
 
