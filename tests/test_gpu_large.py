@@ -134,3 +134,14 @@ def test_shell_mesh_properties(shell):
     # the shell has an outer and an inner (cavity) surface, both inside the grid
     r = np.linalg.norm(v - v.mean(axis=0), axis=1)
     assert r.min() < 400.0 < 430.0 < r.max()
+
+
+def test_shell_smoothing_in_waves_exact(shell):
+    """Smoothing a mesh far above one slab wave (152 x 25 000 vertices): sequential waves,
+    still the sequential Gauss-Seidel result."""
+    xyz, rad, g, m, _ = shell
+    assert len(m.vertices) > 3 * 152 * 25000
+    with q.Context(0) as c:
+        m1 = c.compute(xyz, rad, voxel=SHELL.voxel, smooth=1, keep_degenerate=True)
+    assert np.array_equal(m1.triangles, m.triangles)
+    assert np.array_equal(m1.vertices, O.smooth_f32(m.vertices, m.triangles, 1))
