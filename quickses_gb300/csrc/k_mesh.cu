@@ -777,7 +777,9 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                 for (unsigned base = e0; base < e1; base += 32) {
                     const unsigned m = min(32u, e1 - base);
                     const unsigned u = lane < m ? (base == e0 ? first_id : __ldg(nbr + base + lane)) : 0u;
-                    const bool higher = lane < m && u > v;
+                    // successors at or above nv (the wave's end) belong to a later wave, which
+                    // starts after this one has finished: nothing to release for them
+                    const bool higher = lane < m && u > v && u < nv;
                     const bool remote_edge = higher && u >= b;
                     bool ready = false;
                     if (higher) {
