@@ -208,7 +208,7 @@ def run_gpu(args):
         if rc != 0:
             raise RuntimeError(lib.qses_last_error(ctx.handle).decode())
         h2d = 16 * n
-        d2h = 12 * mesh.n_vertices + 12 * mesh.n_triangles + 8 * mesh.n_vertices
+        d2h = int(lib.qses_last_download_bytes(ctx.handle))  # triangles sized by the pre-filter count
         lib.qses_mesh_release(ctypes.byref(mesh))
         if it >= args.warmup:
             e2e_times.append(dt)

@@ -235,6 +235,9 @@ QSES_API int qses_set_profiling(qses_context *ctx, int on);
 QSES_API int qses_stage_times(qses_context *ctx, float *ms, const char **names, int max);
 /* Number of kernels the last call launched. */
 QSES_API int qses_last_launch_count(qses_context *ctx);
+/* Device-to-host bytes the last qses_compute copied (the triangle download is sized by the
+ * pre-filter count so it can start while the smoothing pass runs). */
+QSES_API unsigned long long qses_last_download_bytes(qses_context *ctx);
 /* Smoothing diagnostics of the last call: [0] slabs, [1] vertices per slab, [2] most
  * boundary polls of one slab, [3] slabs that did not finish, [4] clock cycles spent in
  * vertex updates, [5] in releasing successors, [6] vertices updated, [7] cycles until a

@@ -103,6 +103,7 @@ SIGNATURES = {
     "qses_set_profiling": (ctypes.c_int, [_VP, ctypes.c_int]),
     "qses_stage_times": (ctypes.c_int, [_VP, _FP, ctypes.POINTER(ctypes.c_char_p), ctypes.c_int]),
     "qses_last_launch_count": (ctypes.c_int, [_VP]),
+    "qses_last_download_bytes": (ctypes.c_ulonglong, [_VP]),
     "qses_diagnostics": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
     "qses_field_codes_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_uint, ctypes.c_float, _VP, ctypes.c_size_t,
                                                 _VP]),

@@ -117,6 +117,13 @@ PinnedPool &pinned_pool() {
     return *pool;
 }
 
+}  // namespace
+
+void *qses::pinned_take(size_t bytes, size_t *got) { return pinned_pool().take(bytes, got); }
+void qses::pinned_give(void *p, size_t bytes) { pinned_pool().give(p, bytes); }
+
+namespace {
+
 int fill_host_mesh(qses_context *ctx, qses_mesh *out) {
     const DeviceMesh &m = ctx->mesh;
     memset(out, 0, sizeof(*out));
@@ -141,6 +148,7 @@ int fill_host_mesh(qses_context *ctx, qses_mesh *out) {
         out->grid_dim = ctx->grid.G;
         out->origin[0] = ctx->grid.ox; out->origin[1] = ctx->grid.oy; out->origin[2] = ctx->grid.oz;
     }
+    ctx->last_d2h = vb + tb + 2 * ab;
     cudaStream_t s = ctx->stream;
     cudaError_t e = cudaSuccess;
     if (vb) e = cudaMemcpyAsync(out->vertices, m.vertices, vb, cudaMemcpyDeviceToHost, s);
@@ -222,6 +230,13 @@ QSES_API int qses_context_create(int device, void *cuda_stream, qses_context **o
         }
         ctx->own_stream = true;
     }
+    if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        qses_context_destroy(ctx);
+        return QSES_ERR_CUDA;
+    }
     if (cudaMalloc(&ctx->small, 4096) != cudaSuccess || cudaMallocHost((void **)&ctx->h_small, 4096) != cudaSuccess) {
         cudaGetLastError();
         qses_context_destroy(ctx);
@@ -242,6 +257,11 @@ QSES_API int qses_context_destroy(qses_context *ctx) {
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     for (auto &m : ctx->marks) cudaEventDestroy(m.second);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    if (ctx->dl.block) qses::pinned_give(ctx->dl.block, ctx->dl.bytes);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return QSES_OK;
@@ -262,9 +282,41 @@ QSES_API int qses_compute(qses_context *ctx, const qses_params *p, const qses_fl
     cudaError_t e = cudaMemcpyAsync(d_xyz, atoms, 12ull * n, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_r, radii, 4ull * n, cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) return ctx->fail(QSES_ERR_CUDA, "atom upload", e);
+    ctx->dl = qses::HostDownload();
+    ctx->dl.want = true;
     rc = qses::run_pipeline(ctx, *p, d_xyz, d_r, n);
-    if (rc) return rc;
-    return fill_host_mesh(ctx, out);
+    qses::HostDownload dl = ctx->dl;
+    ctx->dl = qses::HostDownload();
+    if (rc) {
+        if (dl.block) {  // copies into it may still be queued
+            cudaStreamSynchronize(ctx->stream);
+            cudaStreamSynchronize(ctx->side);
+            qses::pinned_give(dl.block, dl.bytes);
+        }
+        return rc;
+    }
+    if (!dl.block) return fill_host_mesh(ctx, out);
+    // the pipeline downloaded the mesh into dl.block while the smoothing pass ran
+    HostMesh *hm = new (std::nothrow) HostMesh();
+    if (!hm) {
+        qses::pinned_give(dl.block, dl.bytes);
+        return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "host mesh");
+    }
+    hm->block = dl.block;
+    hm->bytes = dl.bytes;
+    char *b = (char *)dl.block;
+    const qses::DeviceMesh &m = ctx->mesh;
+    out->vertices = (qses_float3 *)b;
+    out->triangles = (int *)(b + dl.vb);
+    out->atom_sorted = (int *)(b + dl.vb + dl.tb);
+    out->atom_input = (int *)(b + dl.vb + dl.tb + dl.ab);
+    out->n_vertices = m.nv;
+    out->n_triangles = m.nt;
+    out->grid_dim = ctx->grid.G;
+    out->origin[0] = ctx->grid.ox; out->origin[1] = ctx->grid.oy; out->origin[2] = ctx->grid.oz;
+    out->_owner = hm;
+    ctx->last_d2h = dl.d2h;
+    return QSES_OK;
 }
 
 QSES_API int qses_compute_device(qses_context *ctx, const qses_params *p, const float *d_xyz, const float *d_radii,
@@ -595,6 +647,8 @@ QSES_API int qses_stage_times(qses_context *ctx, float *ms, const char **names, 
 }
 
 QSES_API int qses_last_launch_count(qses_context *ctx) { return ctx ? ctx->launches : 0; }
+
+QSES_API unsigned long long qses_last_download_bytes(qses_context *ctx) { return ctx ? ctx->last_d2h : 0ull; }
 
 QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max) {
     if (!ctx || !out) return 0;

@@ -203,7 +203,8 @@ static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 int run_smoothing(qses_context *ctx, const GsShape &sh, int passes, float *vq, float4 *pos4, unsigned nv,
                   const uint2 *deg, const unsigned *nbr, unsigned short *cnt, int *remote, unsigned *inbox,
-                  unsigned *inbox_tail, int *d_err, unsigned long long *stats, bool record_slabs) {
+                  unsigned *inbox_tail, int *d_err, unsigned long long *stats, bool record_slabs,
+                  cudaEvent_t before_writeback) {
     cudaStream_t s = ctx->stream;
     const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts, sh.threads), 1024);
     if (pmax < 1) return ctx->fail(QSES_ERR_NO_DEVICE, "the smoothing kernel does not fit on this device");
@@ -239,6 +240,7 @@ int run_smoothing(qses_context *ctx, const GsShape &sh, int passes, float *vq, f
         }
     }
     if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, nullptr, 0);
+    if (before_writeback) QCHK(cudaStreamWaitEvent(s, before_writeback, 0));
     launch_from_float4(pos4, nv, vq, s);
     ctx->launches++;
     return QSES_OK;
@@ -357,7 +359,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
                    align256(4ull * NE) + align256(12ull * NE) + 2 * align256(4ull * NE) + 2 * align256(4 * n3) +
                    2 * align256(4 * n3) + align256(8 * n3) + 3 * align256(4ull * NE) + align256(4ull * NE + 4096) + 4096 +
                    align256(16ull * NE + 16) +
-                   align256(tmpB) + 4096;
+                   align256(tmpB) + align256(8ull * T + 16) + align256(scan_u2_tmp_bytes(T + 1)) + 4096;
     if (ctx->mesh_ws.reserve(needB) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "mesh workspace");
     Arena &B = ctx->mesh_ws;
     unsigned *tri = (unsigned *)B.take(4 * n3 + 4);
@@ -376,7 +378,9 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     unsigned *inbox_tail = (unsigned *)B.take(4096);
     float4 *pos4 = (float4 *)B.take(16ull * NE + 16);
     void *tmpb = B.take(tmpB);
-    if (!tmpb) return ctx->fail(QSES_ERR_INTERNAL, "mesh workspace layout");
+    uint2 *tflags = (uint2 *)B.take(8ull * T + 16);      // degenerate filter (side stream)
+    void *tmp2 = B.take(scan_u2_tmp_bytes(T + 1));       // its scan's scratch
+    if (!tmpb || !tflags || !tmp2) return ctx->fail(QSES_ERR_INTERNAL, "mesh workspace layout");
 
     // ---- triangles + pre-weld vertex keys
     launch_mc_emit(g, signMask, codes, d_lut, rows, tri, vk, s);
@@ -403,12 +407,51 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     }
     ctx->mark("weld");
 
+    // Closest atom, degenerate filter and (for host results) the triangle and atom-id
+    // downloads run on the side stream while the main stream builds the neighbour lists and
+    // smooths; profiled calls keep one stream so the stage times stay separable.
+    const bool fork = !ctx->profiling && ctx->side != nullptr;
+    cudaStream_t sd = fork ? ctx->side : s;
+    const bool keep_all = (p.flags & QSES_FLAG_KEEP_DEGENERATE) != 0;
+    HostDownload &dl = ctx->dl;
+    if (dl.want) {  // [vertices | triangles (pre-filter count) | atom_sorted | atom_input]
+        dl.vb = 12ull * nv;
+        dl.tb = 12ull * T;
+        dl.ab = 4ull * nv;
+        dl.block = pinned_take(dl.vb + dl.tb + 2 * dl.ab + 64, &dl.bytes);
+        if (!dl.block) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned host mesh");
+    }
+    if (fork) {
+        QCHK(cudaEventRecord(ctx->ev_fork, s));
+        QCHK(cudaStreamWaitEvent(sd, ctx->ev_fork, 0));
+    }
+
     // ---- closest atom per welded vertex (before smoothing, as in the reference)
     if (nv > 0) {
-        launch_closest(g, vq, nv, atoms, cells, sidx, asorted, ainput, s);
+        launch_closest(g, vq, nv, atoms, cells, sidx, asorted, ainput, sd);
         ctx->launches++;
     }
     ctx->mark("closest_atom");
+
+    // ---- drop degenerate triangles (API_computeSES filter)
+    if (!keep_all && T > 0) {
+        launch_tri_flags(tri, T, tflags, sd);
+        ctx->launches++;
+        QCHK(scan_u2(tflags, tflags, T, d_tot, tmp2, d_err, sd, &ctx->launches));
+        launch_tri_compact(tri, T, tflags, tri_kept, sd);
+        ctx->launches++;
+        QCHK(cudaMemcpyAsync(ctx->h_small, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, sd));
+    }
+    ctx->mark("filter");
+    const unsigned *tri_out = keep_all ? tri : tri_kept;
+    if (dl.want) {
+        char *hb = (char *)dl.block;
+        if (dl.tb) QCHK(cudaMemcpyAsync(hb + dl.vb, tri_out, dl.tb, cudaMemcpyDeviceToHost, sd));
+        if (dl.ab) QCHK(cudaMemcpyAsync(hb + dl.vb + dl.tb, asorted, dl.ab, cudaMemcpyDeviceToHost, sd));
+        if (dl.ab) QCHK(cudaMemcpyAsync(hb + dl.vb + dl.tb + dl.ab, ainput, dl.ab, cudaMemcpyDeviceToHost, sd));
+        dl.d2h = dl.tb + 2 * dl.ab;
+    }
+    if (fork) QCHK(cudaEventRecord(ctx->ev_join, sd));
 
     // ---- Gauss-Seidel smoothing on the device
     if (p.smooth_passes > 0 && nv > 0 && T > 0) {
@@ -428,28 +471,24 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         const GsShape sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(nv, false);
         ctx->gs_used = sh;
         unsigned long long *stats = (unsigned long long *)((char *)ctx->small + 256);
+        // the closest-atom pass on the side stream reads the welded positions in vq
         int rc2 = run_smoothing(ctx, sh, p.smooth_passes, vq, pos4, nv, deg, nbr, (unsigned short *)cnt, lower, inbox,
-                                inbox_tail, d_err, stats, true);
+                                inbox_tail, d_err, stats, true, fork ? ctx->ev_join : nullptr);
         if (rc2) return rc2;
     }
     ctx->mark("smooth");
-
-    // ---- drop degenerate triangles (API_computeSES filter)
-    unsigned nkept = T;
-    const bool keep_all = (p.flags & QSES_FLAG_KEEP_DEGENERATE) != 0;
-    if (!keep_all && T > 0) {
-        launch_tri_flags(tri, T, flags, s);
-        ctx->launches++;
-        QCHK(scan_u2(flags, flags, T, d_tot, tmpb, d_err, s, &ctx->launches));
-        launch_tri_compact(tri, T, flags, tri_kept, s);
-        ctx->launches++;
-        QCHK(cudaMemcpyAsync(ctx->h_small, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    if (dl.want && dl.vb) {
+        QCHK(cudaMemcpyAsync(dl.block, vq, dl.vb, cudaMemcpyDeviceToHost, s));
+        dl.d2h += dl.vb;
     }
+    if (fork) QCHK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+
     QCHK(cudaMemcpyAsync(ctx->h_small + 8, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     QCHK(cudaMemcpyAsync(ctx->h_small + 2048, (char *)ctx->small + 256, 64, cudaMemcpyDeviceToHost, s));
     QCHK(cudaStreamSynchronize(s));
-    ctx->mark("filter");
+    ctx->mark("download");
     memcpy(ctx->diag + 2, ctx->h_small + 2048, 7 * sizeof(unsigned long long));
+    unsigned nkept = T;
     if (!keep_all && T > 0) {
         memcpy(&tot, ctx->h_small, sizeof(tot));
         nkept = tot.x;

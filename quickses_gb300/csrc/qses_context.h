@@ -56,10 +56,28 @@ struct BatchResult {
 
 }  // namespace qses
 
+namespace qses {
+// Pinned host blocks from the process-wide cache (released blocks are reused).
+void *pinned_take(size_t bytes, size_t *got);
+void pinned_give(void *p, size_t bytes);
+
+// Host destination of a qses_compute call, filled by the pipeline while the smoothing pass
+// still runs: [vertices 12 nv | triangles 12 T (upper bound) | atom_sorted 4 nv | atom_input 4 nv].
+struct HostDownload {
+    bool want = false;
+    void *block = nullptr;
+    size_t bytes = 0, vb = 0, tb = 0, ab = 0;
+    unsigned long long d2h = 0;  // bytes copied
+};
+}  // namespace qses
+
 struct qses_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    cudaStream_t side = nullptr;          // closest atom, filter and downloads beside the smoothing
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    qses::HostDownload dl;
     qses::Arena input, field, mesh_ws;
     void *small = nullptr;            // 4 KB device scratch: bounds, error word, queue counters
     unsigned char *h_small = nullptr; // 4 KB pinned host scratch
@@ -75,6 +93,7 @@ struct qses_context {
     std::vector<std::pair<const char *, cudaEvent_t>> marks;
     std::vector<std::pair<const char *, float>> times;
     int launches = 0;
+    unsigned long long last_d2h = 0;  // device-to-host bytes of the last qses_compute
     qses::GsShape gs_force{0, 0, 0, 0};  // autotuner: forced smoothing shape (threads 0 = none)
     qses::GsShape gs_used;            // shape of the last smoothing run
     int edt_force = -1;               // autotuner: forced refine tile shape (-1 = none)
@@ -91,9 +110,12 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
 // and out, CSR (deg offsets, nbr), shape sh.  The vertices run in sequential waves of at
 // most the slab kernel's capacity; every dependency points to a lower id, so a wave only
 // depends on earlier, finished waves.
+// `before_writeback` (may be null): event the stream waits for before the smoothed
+// positions overwrite vq (work on another stream that still reads the welded positions).
 int run_smoothing(qses_context *ctx, const GsShape &sh, int passes, float *vq, float4 *pos4, unsigned nv,
                   const uint2 *deg, const unsigned *nbr, unsigned short *cnt, int *remote, unsigned *inbox,
-                  unsigned *inbox_tail, int *d_err, unsigned long long *stats, bool record_slabs);
+                  unsigned *inbox_tail, int *d_err, unsigned long long *stats, bool record_slabs,
+                  cudaEvent_t before_writeback = nullptr);
 // All items share `passes`; the weld keys of every item fit `key_bits` bits and
 // key_bits + bits(count - 1) <= 64.  Results in ctx->batch.
 int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int passes, int key_bits);
