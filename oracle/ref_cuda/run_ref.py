@@ -7,6 +7,7 @@ TEST INFRASTRUCTURE ONLY.  Needs oracle/_ref/libQuickSES.so and oracle/_ref/libr
     python oracle/ref_cuda/run_ref.py field                    # reference field vs our voxel codes
     python oracle/ref_cuda/run_ref.py fixtures                 # tests/golden/ref_cuda.npz
     python oracle/ref_cuda/run_ref.py stream batched|trajectory|served   # plain path, molecules/s
+    python oracle/ref_cuda/run_ref.py smooth ball50k           # SmoothMesh.cpp on the CPU vs ours
 
 Timing is wall clock around the reference's API_computeSES (its whole library call:
 upload, slices, host smoothing, concatenation) and around our qses_compute (upload,
@@ -215,6 +216,55 @@ def fixtures(out=os.path.join(ROOT, "tests", "golden", "ref_cuda.npz")):
     print("wrote", out, os.path.getsize(out))
 
 
+def time_only(names):
+    """Wall clock of the reference's API_computeSES and of our qses_compute on one workload,
+    with mesh counts (no distance computation: for the largest workloads)."""
+    ref = Ref()
+    with q.Context(0) as ctx:
+        for name in names:
+            wl = q.molecules.WORKLOADS[name]
+            xyz, rad, _ = wl.atoms()
+            G = q.grid_info(xyz, rad, wl.voxel).G
+            ours = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                mo = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=wl.smooth)
+                ours.append(time.perf_counter() - t0)
+            vr, tr, _, ref_t = ref.compute(xyz, rad, wl.voxel, wl.smooth)
+            print(json.dumps({"workload": name, "grid": G, "voxels": G ** 3, "ref_s": ref_t, "ours_s": min(ours),
+                              "speedup": ref_t / min(ours), "ref_vertices": len(vr), "ref_triangles": len(tr),
+                              "our_vertices": len(mo.vertices), "our_triangles": len(mo.triangles)}), flush=True)
+
+
+def smooth(names):
+    """The reference's CPU smoothing (SmoothMesh.cpp, single-threaded, compiled from the
+    staged sources by oracle/build.py) on our unsmoothed mesh: its time, and whether our
+    GPU pass gives the same positions bit for bit."""
+    from oracle import build as ob
+    path = ob.build_ref(ref=os.path.join(REF, "src"))
+    L = ctypes.CDLL(path)
+    L.ref_smooth.restype = None
+    L.ref_smooth.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint]
+    with q.Context(0) as ctx:
+        for name in names:
+            wl = q.molecules.WORKLOADS[name]
+            xyz, rad, _ = wl.atoms()
+            m0 = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=0, keep_degenerate=True)
+            ctx.set_profiling(True)
+            m1 = ctx.compute(xyz, rad, voxel=wl.voxel, smooth=1, keep_degenerate=True)
+            gpu_ms = dict(ctx.stage_times()).get("smooth")
+            ctx.set_profiling(False)
+            v = np.ascontiguousarray(m0.vertices.copy())
+            t = np.ascontiguousarray(m0.triangles, np.int32)
+            t0 = time.perf_counter()
+            L.ref_smooth(1, v.ctypes.data, t.ctypes.data, len(v), len(t))
+            ref_s = time.perf_counter() - t0
+            print(json.dumps({"workload": name, "vertices": len(v), "triangles": len(t), "ref_smooth_s": ref_s,
+                              "ref_threads": 1, "gpu_smooth_ms": gpu_ms,
+                              "speedup": ref_s / (gpu_ms * 1e-3) if gpu_ms else None,
+                              "bit_identical": bool(np.array_equal(v, m1.vertices))}), flush=True)
+
+
 def stream(which, limit=None):
     """The reference's plain path (one API_computeSES per molecule, wall clock per call) on
     the request streams of the batch and served forms; prints molecules/s."""
@@ -239,6 +289,12 @@ if __name__ == "__main__":
     mode = sys.argv[1]
     if mode == "stream":
         stream(sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else None)
+        sys.exit(0)
+    if mode == "time":
+        time_only(sys.argv[2:])
+        sys.exit(0)
+    if mode == "smooth":
+        smooth(sys.argv[2:] or ["ball50k"])
         sys.exit(0)
     if mode == "compare":
         compare(sys.argv[2:] or ["ball1k"])
