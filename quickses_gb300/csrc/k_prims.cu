@@ -88,7 +88,10 @@ cudaError_t scan_u2(const uint2 *in, uint2 *out, unsigned n, uint2 *d_total, voi
 }
 
 // ------------------------------------------------------------ radix sort
-constexpr int kRsT = 256, kRsI = 16, kRsTile = kRsT * kRsI, kRsW = kRsT / 32;
+constexpr int kRsT = 256, kRsW = kRsT / 32;
+// Items per thread: the tile is staged in shared memory before it is written out, so 64-bit
+// keys take fewer per thread (static shared memory stays under 48 KB).
+template <typename K> struct RsTile { static constexpr int kItems = sizeof(K) == 8 ? 12 : 16; };
 
 template <typename K>
 __global__ void __launch_bounds__(256) k_rs_hist(const K *keys, unsigned n, int npass, unsigned *hist) {
@@ -104,26 +107,33 @@ __global__ void __launch_bounds__(256) k_rs_hist(const K *keys, unsigned n, int 
         if (sh[q]) atomicAdd(&hist[q], sh[q]);
 }
 
+// One onesweep pass over a tile of kRsT x kItems keys: stable ranks by warp-level digit
+// matching, the tile's offset per digit by decoupled look-back over tiles, then the tile is
+// reordered by digit in shared memory so each digit's run is written out contiguously.
 template <typename K>
 __global__ void __launch_bounds__(kRsT) k_rs_pass(const K *__restrict__ kin, K *__restrict__ kout,
                                                   const unsigned *__restrict__ vin, unsigned *__restrict__ vout,
                                                   unsigned n, int shift, const unsigned *__restrict__ hist,
                                                   unsigned long long *status, unsigned *ticket, int *err) {
+    constexpr int I = RsTile<K>::kItems, TILE = kRsT * I;
     __shared__ unsigned s_wc[kRsW][256];
-    __shared__ unsigned s_base[256];
+    __shared__ unsigned s_base[256], s_lstart[256];
     __shared__ unsigned s_tmp[kRsT / 32];
     __shared__ unsigned s_tile;
+    __shared__ K s_key[TILE];
+    __shared__ unsigned s_val[TILE];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
     for (int q = tid; q < kRsW * 256; q += kRsT) (&s_wc[0][0])[q] = 0;
     __syncthreads();
     const unsigned tile = s_tile;
-    const size_t wbase = (size_t)tile * kRsTile + (size_t)warp * (32 * kRsI);
+    const size_t tbase = (size_t)tile * TILE;
+    const size_t wbase = tbase + (size_t)warp * (32 * I);
 
-    K key[kRsI];
-    unsigned val[kRsI], dig[kRsI], rank[kRsI];
+    K key[I];
+    unsigned val[I], dig[I], rank[I];
 #pragma unroll
-    for (int it = 0; it < kRsI; it++) {
+    for (int it = 0; it < I; it++) {
         size_t idx = wbase + (size_t)it * 32 + lane;
         if (idx < n) {
             key[it] = kin[idx];
@@ -137,7 +147,7 @@ __global__ void __launch_bounds__(kRsT) k_rs_pass(const K *__restrict__ kin, K *
     }
     // Stable rank within the warp's contiguous segment, item by item in input order.
 #pragma unroll
-    for (int it = 0; it < kRsI; it++) {
+    for (int it = 0; it < I; it++) {
         const unsigned d = dig[it];
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const unsigned lower = peers & ((1u << lane) - 1u);
@@ -170,26 +180,37 @@ __global__ void __launch_bounds__(kRsT) k_rs_pass(const K *__restrict__ kin, K *
         }
         st_release(st, kFlagPre | (unsigned long long)(excl + run));
     }
-    unsigned htot;
-    unsigned dstart = block_excl_scan<kRsT>(hist[d], htot, s_tmp);
-    s_base[d] = dstart + excl;
+    unsigned htot, ltot;
+    const unsigned dstart = block_excl_scan<kRsT>(hist[d], htot, s_tmp);
+    const unsigned lstart = block_excl_scan<kRsT>(run, ltot, s_tmp);
+    s_base[d] = dstart + excl;  // global position of this tile's first key of digit d
+    s_lstart[d] = lstart;       // its position within the digit-sorted tile
     __syncthreads();
 #pragma unroll
-    for (int it = 0; it < kRsI; it++) {
+    for (int it = 0; it < I; it++) {
         const unsigned dd = dig[it];
         if (dd < 256) {
-            unsigned pos = s_base[dd] + s_wc[warp][dd] + rank[it];
-            if (pos < n) {
-                kout[pos] = key[it];
-                vout[pos] = val[it];
-            }
+            const unsigned lp = s_lstart[dd] + s_wc[warp][dd] + rank[it];
+            s_key[lp] = key[it];
+            s_val[lp] = val[it];
+        }
+    }
+    __syncthreads();
+    // ltot keys of this tile, digit-sorted: consecutive threads write consecutive addresses.
+    for (unsigned q = tid; q < ltot; q += kRsT) {
+        const K k = s_key[q];
+        const unsigned dd = (unsigned)((k >> shift) & 255);
+        const unsigned pos = s_base[dd] + (q - s_lstart[dd]);
+        if (pos < n) {
+            kout[pos] = k;
+            vout[pos] = s_val[q];
         }
     }
 }
 
 size_t radix_sort_tmp_bytes(unsigned n, int bits) {
     int npass = (bits + 7) / 8;
-    size_t tiles = (n + kRsTile - 1) / kRsTile;
+    size_t tiles = (n + kRsT * 12 - 1) / (kRsT * 12);  // the smaller (64-bit key) tile bounds both
     return 256 + (size_t)npass * 256 * sizeof(unsigned) + tiles * 256 * sizeof(unsigned long long);
 }
 
@@ -201,7 +222,8 @@ cudaError_t radix_sort(K *keys, K *keys_alt, unsigned *vals, unsigned *vals_alt,
     if (npass > (int)sizeof(K)) npass = (int)sizeof(K);
     if (n == 0) return cudaSuccess;
     if (npass == 0) npass = 1;  // still materialise the values (identity case)
-    unsigned tiles = (n + kRsTile - 1) / kRsTile;
+    constexpr unsigned kTile = kRsT * RsTile<K>::kItems;
+    unsigned tiles = (n + kTile - 1) / kTile;
     unsigned *ticket = (unsigned *)tmp;
     unsigned *hist = (unsigned *)((char *)tmp + 256);
     unsigned long long *status = (unsigned long long *)((char *)hist + (size_t)npass * 256 * sizeof(unsigned));
