@@ -185,15 +185,44 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
         const unsigned p2 = grp_incl_scan(c10, sub, Lg) - c10, p3 = grp_incl_scan(c11, sub, Lg) - c11;
         const unsigned tp = grp_incl_scan(ntri, sub, Lg) - ntri;
 
-        // Vertices owned by this row, in voxel order, x then y then z within a voxel.
+        // Vertices owned by this row, in voxel order, x then y then z within a voxel: edge e of
+        // the group's words goes to slot eb0 + ec0 + e.  The few words a surface crosses hold
+        // all of a row's edges, so the edges are dealt out over the group's lanes: lane `sub`
+        // takes e = sub, sub + Lg, ..., finds the owning lane (largest L with p0[L] <= e) and
+        // the voxel and axis of the edge inside that lane's word.
         {
-            unsigned slot = eb0 + ec0 + p0;
-            for (unsigned m = X00 | Y00 | Z00; m; m &= m - 1u) {
-                const unsigned b = __ffs(m) - 1;
-                const int k = kb + (int)b;
-                if ((X00 >> b) & 1u) vkey[slot++] = keyhi + edge_key(g, codes, lut, i, j, k, 0);
-                if ((Y00 >> b) & 1u) vkey[slot++] = keyhi + edge_key(g, codes, lut, i, j, k, 1);
-                if ((Z00 >> b) & 1u) vkey[slot++] = keyhi + edge_key(g, codes, lut, i, j, k, 2);
+            const unsigned etot = grp_sum(c00, Lg);
+            const unsigned emax = FULL ? etot : __reduce_max_sync(0xffffffffu, etot);  // warp-uniform
+            const int gbase = (int)(threadIdx.x & 31) & ~(Lg - 1);
+            for (unsigned eb = 0; eb < emax; eb += (unsigned)Lg) {
+                const unsigned e = eb + (unsigned)sub;
+                int lo = 0;
+                for (int step = Lg >> 1; step > 0; step >>= 1) {
+                    const unsigned pl = __shfl_sync(0xffffffffu, p0, gbase + lo + step);
+                    if (pl <= e) lo += step;
+                }
+                const unsigned Xo = __shfl_sync(0xffffffffu, X00, gbase + lo);
+                const unsigned Yo = __shfl_sync(0xffffffffu, Y00, gbase + lo);
+                const unsigned Zo = __shfl_sync(0xffffffffu, Z00, gbase + lo);
+                const unsigned po = __shfl_sync(0xffffffffu, p0, gbase + lo);
+                if (e < etot) {
+                    const unsigned r = e - po;  // rank of the edge inside the owner's word
+                    int b = 0;                  // its voxel: the largest b with fewer than r+1 edges below
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const unsigned lt = (1u << (b + step)) - 1u;
+                        if ((unsigned)(__popc(Xo & lt) + __popc(Yo & lt) + __popc(Zo & lt)) <= r) b += step;
+                    }
+                    const unsigned lt = (1u << b) - 1u;
+                    unsigned qa = r - (unsigned)(__popc(Xo & lt) + __popc(Yo & lt) + __popc(Zo & lt));
+                    int ax = 2;
+                    if ((Xo >> b) & 1u) {
+                        if (qa == 0) ax = 0;
+                        else qa--;
+                    }
+                    if (ax == 2 && ((Yo >> b) & 1u) && qa == 0) ax = 1;
+                    const int k = (w0 + lo) * 32 + b;
+                    vkey[eb0 + ec0 + e] = keyhi + edge_key(g, codes, lut, i, j, k, ax);
+                }
             }
         }
         // Triangles in cell order, corners as pre-weld vertex slots.
@@ -257,7 +286,7 @@ __global__ void __launch_bounds__(256, 3) k_mc(QGrid g, const unsigned *__restri
 // every molecule's triangles and edge slots contiguous ranges in molecule order.  Each warp
 // takes one unit of 32 / Lg rows of one molecule (units numbered by mc_unit_off).
 template <bool EMIT>
-__global__ void __launch_bounds__(256) k_mc_batch(QBatch b, const unsigned *__restrict__ sign,
+__global__ void __launch_bounds__(256, 2) k_mc_batch(QBatch b, const unsigned *__restrict__ sign,
                                                   const unsigned char *__restrict__ codes, uint2 *__restrict__ rowCount,
                                                   const uint2 *__restrict__ rowBase, unsigned *__restrict__ tri,
                                                   unsigned long long *__restrict__ vkey) {
