@@ -8,11 +8,11 @@ single-molecule configuration.  voxels = G^3 of the reference's grid sizing.
 * e2e       same metric through the C-ABI with host buffers (qses_compute: atom upload,
             full pipeline, mesh download into library-owned pinned buffers)
 * roofline  dominant stage: algorithmic bytes / its CUDA-event time vs measured HBM peak
-* cpu_baseline  the CPU oracle on a bounded slab of the same grid, all host threads
+* cpu_baseline  the CPU oracle (all host threads) on the same molecule: the whole pipeline
 
 `--impl reference` times the reference path's CPU implementation instead: QuickSES has no
 CPU field code, so this is the CPU oracle port (C++/OpenMP restatement) on the same
-workload, one bounded slab per step.
+workload, the whole pipeline per step.
 """
 import argparse
 import ctypes
@@ -284,18 +284,24 @@ def run_once(args):
 
 
 def cpu_baseline(wl, xyz, rad, planes):
-    """The CPU oracle (FP32 mode, all host threads): SAS classification + probe refine for
-    `planes` x-planes of the grid (default: all of them; the refine halo is included in the
-    work).  Marching cubes, weld and smoothing are left out, so this overstates the CPU's
-    end-to-end rate.  voxels/s = voxels covered / time."""
+    """The CPU oracle (FP32 mode, all host threads) on the whole workload: SAS + refine
+    field, marching cubes, weld, closest atom and the sequential Gauss-Seidel pass - the same
+    job as one GPU step.  With `planes` > 0, only the field of that many x-planes (a
+    smaller sample for slow hosts).  voxels/s = voxels covered / time."""
     from oracle import oracle as O
     g, _ = O.grid(xyz, rad, wl.voxel)
-    planes = g.G if planes <= 0 or planes > g.G else planes
+    cores = os.cpu_count()
+    if planes <= 0 or planes >= g.G:
+        t0 = time.perf_counter()
+        m = O.compute_ses(xyz, rad, wl.voxel, smooth=wl.smooth, fp64=False)
+        dt = time.perf_counter() - t0
+        return {"value": float(g.G) ** 3 / dt, "unit": "voxels/s", "cores": cores, "kind": "port",
+                "sample": "oracle full pipeline on the whole %d^3 grid (field, marching cubes, weld, closest atom, "
+                          "%d Gauss-Seidel pass, %d vertices): %.1f s" % (g.G, wl.smooth, len(m.vertices), dt)}
     x0 = g.G // 2 - planes // 2
     t0 = time.perf_counter()
     O.field_codes(xyz, rad, g, fp64=False, x0=x0, x1=x0 + planes)
     dt = time.perf_counter() - t0
-    cores = os.cpu_count()
     return {"value": planes * g.G * g.G / dt, "unit": "voxels/s", "cores": cores, "kind": "port",
             "sample": "oracle SAS+refine on x-planes [%d,%d) of the %d^3 grid (%.1f s); MC/weld/smoothing "
                       "not included" % (x0, x0 + planes, g.G, dt)}
@@ -306,27 +312,24 @@ def run_reference(args):
     if rank != 0:
         return
     import quickses_gb300 as q
-    from oracle import oracle as O
     wl = q.molecules.WORKLOADS[args.workload]
     xyz, rad, _ = wl.atoms()
-    g, _ = O.grid(xyz, rad, wl.voxel)
-    planes = g.G if args.cpu_planes <= 0 or args.cpu_planes > g.G else args.cpu_planes
-    x0 = g.G // 2 - planes // 2
-    times = []
+    times, last = [], None
     for it in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        O.field_codes(xyz, rad, g, fp64=False, x0=x0, x1=x0 + planes)
-        dt = time.perf_counter() - t0
+        res = cpu_baseline(wl, xyz, rad, args.cpu_planes)
+        last = res
         if it >= args.warmup:
-            times.append(dt)
-    sec = float(np.mean(times))
-    v = planes * g.G * g.G / sec
-    sample = ("CPU oracle port (C++/OpenMP restatement of the reference grid method; the reference ships no CPU "
-              "field code): SAS+refine on %d of %d x-planes per step" % (planes, g.G))
+            times.append(res["value"])
+    v = float(np.mean(times))
+    g = q.grid_info(xyz, rad, wl.voxel)
+    sample = ("CPU oracle port (C++/OpenMP restatement of the reference path; the reference ships no CPU field "
+              "code, and its CPU smoothing is the same sequential Gauss-Seidel loop): " + last["sample"])
     out = {"impl": "reference", "metric": "SES grid voxels/s per molecule", "value": v, "unit": "voxels/s",
-           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": float(g.G) ** 3 / v * 1e3 if args.cpu_planes <= 0 else None,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "%s: %d atoms, voxel %.2f A, grid %d^3" % (wl.name, len(rad), wl.voxel, g.G)},
+           "config": {"workload": "%s: %d atoms, voxel %.2f A, %d smoothing pass, grid %d^3"
+                                  % (wl.name, len(rad), wl.voxel, wl.smooth, g.G)},
            "cpu_baseline": {"value": v, "unit": "voxels/s", "cores": os.cpu_count(), "kind": "port",
                             "sample": sample},
            "e2e": {"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -492,7 +495,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ball50k")
-    ap.add_argument("--cpu-planes", type=int, default=0, help="x-planes of the CPU sample (0 = whole grid)")
+    ap.add_argument("--cpu-planes", type=int, default=0, help="CPU sample: 0 = the whole pipeline on the whole molecule (default); N > 0 = "
+                         "only the field of N x-planes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", default="plain", choices=["plain", "batched", "trajectory", "served"],
                     help="plain: one molecule per step (default); batched/trajectory: a molecule stream per step "
