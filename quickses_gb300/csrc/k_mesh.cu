@@ -752,6 +752,9 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                 __nanosleep(20);
                 continue;
             }
+            // Neighbour ids of the vertex this warp continues with, loaded as soon as the
+            // release picked it (the lists are constant, so the early load is always valid).
+            unsigned pre_v = 0xffffffffu, pre_id = 0u;
             while (v != 0xffffffffu) {  // follow the chain of vertices this warp releases
                 __threadfence_block();
                 const long long c0 = clock64();
@@ -760,7 +763,8 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                 unsigned first_id = v;
                 for (unsigned base = e0; base < e1; base += 32) {
                     const unsigned m = min(32u, e1 - base);
-                    const unsigned id = lane < m ? __ldg(nbr + base + lane) : v;
+                    const unsigned id = (base == e0 && pre_v == v) ? pre_id
+                                                                  : (lane < m ? __ldg(nbr + base + lane) : v);
                     if (base == e0) first_id = id;
                     long long ca = 0;
                     if (stats && base == e0) {  // diagnostics: when the ids have arrived
@@ -836,6 +840,9 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                         const unsigned f = __ffs(mask) - 1;
                         next = __shfl_sync(0xffffffffu, u, f);  // continue with it directly
                         mask &= ~(1u << f);
+                        const unsigned ne0 = st[next - a], nm = min(32u, st[next - a + 1] - ne0);
+                        pre_id = lane < nm ? __ldg(nbr + ne0 + lane) : next;
+                        pre_v = next;
                     }
                     if ((mask >> lane) & 1u) ring_push16(ring, &s_tail, u - a);
                 }
