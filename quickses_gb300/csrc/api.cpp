@@ -383,23 +383,33 @@ int size_request(const qses_request &r, QGrid &g) {
 int fill_batch_meshes(qses_context *ctx, const std::vector<unsigned> &reqs, const std::vector<qses::BatchItem> &items,
                       qses_mesh *out) {
     const qses::BatchResult &R = ctx->batch;
-    const size_t vb = 12ull * R.nv, tb = 12ull * R.nkept, ab = 4ull * R.nv;
-    const size_t total = vb + tb + 2 * ab + 256;
-    size_t got = 0;
-    void *block = pinned_pool().take(total, &got);
-    if (!block) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned batch meshes");
-    char *p = (char *)block;
-    cudaStream_t s = ctx->stream;
-    cudaError_t e = cudaSuccess;
-    if (vb) e = cudaMemcpyAsync(p, R.vertices, vb, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && tb) e = cudaMemcpyAsync(p + vb, R.triangles, tb, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && ab) e = cudaMemcpyAsync(p + vb + tb, R.atom_sorted, ab, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && ab) e = cudaMemcpyAsync(p + vb + tb + ab, R.atom_input, ab, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        pinned_pool().give(block, got);
-        return ctx->fail(QSES_ERR_CUDA, "batch mesh download", e);
+    size_t vb = 12ull * R.nv, tb = 12ull * R.nkept, ab = 4ull * R.nv, got = 0;
+    void *block = nullptr;
+    if (ctx->dl.block) {  // downloaded by the pipeline while the smoothing pass ran
+        block = ctx->dl.block;
+        got = ctx->dl.bytes;
+        tb = ctx->dl.tb;  // room for the pre-filter count; the first nkept are the kept ones
+        ctx->last_d2h = ctx->dl.d2h;
+        ctx->dl = qses::HostDownload();
+    } else {
+        block = pinned_pool().take(vb + tb + 2 * ab + 256, &got);
+        if (!block) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned batch meshes");
+        char *p = (char *)block;
+        cudaStream_t s = ctx->stream;
+        cudaError_t e = cudaSuccess;
+        if (vb) e = cudaMemcpyAsync(p, R.vertices, vb, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && tb) e = cudaMemcpyAsync(p + vb, R.triangles, tb, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && ab) e = cudaMemcpyAsync(p + vb + tb, R.atom_sorted, ab, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && ab)
+            e = cudaMemcpyAsync(p + vb + tb + ab, R.atom_input, ab, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            pinned_pool().give(block, got);
+            return ctx->fail(QSES_ERR_CUDA, "batch mesh download", e);
+        }
+        ctx->last_d2h = vb + tb + 2 * ab;
     }
+    char *p = (char *)block;
     std::atomic<int> *refs = new std::atomic<int>((int)reqs.size());
     for (size_t m = 0; m < reqs.size(); m++) {
         qses_mesh &o = out[reqs[m]];
@@ -467,8 +477,17 @@ QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, uns
                 items[m].flags = (unsigned)r.flags;
                 items[m].g = grids[chunk[m]];
             }
+            ctx->dl = qses::HostDownload();
+            ctx->dl.want = true;
             int rc = qses::run_batch(ctx, items.data(), (unsigned)items.size(), grp.first, kb);
+            if (rc != QSES_OK && ctx->dl.block) {  // copies into it may still be queued
+                cudaStreamSynchronize(ctx->stream);
+                cudaStreamSynchronize(ctx->side);
+                qses::pinned_give(ctx->dl.block, ctx->dl.bytes);
+                ctx->dl = qses::HostDownload();
+            }
             if (rc == QSES_OK) rc = fill_batch_meshes(ctx, chunk, items, out);
+            ctx->dl = qses::HostDownload();
             if (rc != QSES_OK) {
                 for (unsigned i : chunk) {
                     if (status) status[i] = rc;

@@ -232,7 +232,8 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     const size_t needB = 2 * a256(4 * n3 + 4) + 2 * a256(8ull * NE + 8) + 2 * a256(4ull * NE + 4) +
                          a256(8ull * nflag) + a256(4ull * NE + 4) + a256(12ull * NE + 12) + 3 * a256(4ull * NE + 4) +
                          4 * a256(4 * n3 + 4) + a256(8 * n3 + 8) + 3 * a256(4ull * NE + 4) + a256(4ull * NE + 65536) +
-                         a256(4096) + a256(16ull * NE + 16) + a256(tmpB) + 8192;
+                         a256(4096) + a256(16ull * NE + 16) + a256(tmpB) + a256(8ull * T + 16) +
+                         a256(scan_u2_tmp_bytes(T + 1)) + 8192;
     if (ctx->mesh_ws.reserve(needB) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "batch mesh workspace");
     Arena &B = ctx->mesh_ws;
     unsigned *tri = (unsigned *)B.take(4 * n3 + 4);
@@ -252,7 +253,9 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     unsigned *inbox_tail = (unsigned *)B.take(4096);
     float4 *pos4 = (float4 *)B.take(16ull * NE + 16);
     void *tmpb = B.take(tmpB);
-    if (!tmpb) return ctx->fail(QSES_ERR_INTERNAL, "batch mesh workspace layout");
+    uint2 *tflags = (uint2 *)B.take(8ull * T + 16);  // degenerate filter (side stream)
+    void *tmp2 = B.take(scan_u2_tmp_bytes(T + 1));   // its scan's scratch
+    if (!tmpb || !tflags || !tmp2) return ctx->fail(QSES_ERR_INTERNAL, "batch mesh workspace layout");
 
     // ---- triangles + molecule-tagged weld keys, then one weld for all molecules
     launch_mc_emit_batch(b, (unsigned)units, signMask, codes, rowsb, tri, vk, s);
@@ -286,11 +289,53 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     nv = NE > 0 ? hsm[0] : 0;
     ctx->mark("weld");
 
+    // Closest atom, filter and (for host results) the triangle and atom-id downloads run on
+    // the side stream beside the neighbour-list build and the smoothing; profiled calls keep
+    // one stream so the stage times stay separable.
+    const bool fork = !ctx->profiling && ctx->side != nullptr;
+    cudaStream_t sd = fork ? ctx->side : s;
+    HostDownload &dl = ctx->dl;
+    if (dl.want) {  // [vertices | triangles (pre-filter count) | atom_sorted | atom_input]
+        dl.vb = 12ull * nv;
+        dl.tb = 12ull * T;
+        dl.ab = 4ull * nv;
+        dl.block = pinned_take(dl.vb + dl.tb + 2 * dl.ab + 256, &dl.bytes);
+        if (!dl.block) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned batch meshes");
+    }
+    if (fork) {
+        QCHK(cudaEventRecord(ctx->ev_fork, s));
+        QCHK(cudaStreamWaitEvent(sd, ctx->ev_fork, 0));
+    }
     if (nv > 0) {
-        launch_closest_batch(b, vq, vmol, nv, atoms, cells, sidx, asorted, ainput, s);
+        launch_closest_batch(b, vq, vmol, nv, atoms, cells, sidx, asorted, ainput, sd);
         ctx->launches++;
     }
     ctx->mark("closest_atom");
+
+    // ---- per-molecule filter and molecule-local corner ids
+    if (T > 0) {
+        launch_tri_flags_batch(b, tri, T, tflags, sd);
+        ctx->launches++;
+        QCHK(scan_u2(tflags, tflags, T, d_tot, tmp2, d_err, sd, &ctx->launches));
+        launch_tri_compact_batch(b, tri, T, tflags, tri_kept, sd);
+        ctx->launches++;
+        launch_gather_offsets(tflags, d_tri_off, nm, T, d_tot, d_kept_off, nullptr, sd);
+        ctx->launches++;
+    } else {
+        QCHK(cudaMemsetAsync(d_kept_off, 0, 4ull * (nm + 1), sd));
+        QCHK(cudaMemsetAsync(d_tot, 0, sizeof(uint2), sd));
+    }
+    QCHK(cudaMemcpyAsync(hsm, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, sd));
+    QCHK(cudaMemcpyAsync(ctx->h_stage, d_kept_off, 4ull * (nm + 1), cudaMemcpyDeviceToHost, sd));
+    ctx->mark("filter");
+    if (dl.want) {
+        char *hb = (char *)dl.block;
+        if (dl.tb) QCHK(cudaMemcpyAsync(hb + dl.vb, tri_kept, dl.tb, cudaMemcpyDeviceToHost, sd));
+        if (dl.ab) QCHK(cudaMemcpyAsync(hb + dl.vb + dl.tb, asorted, dl.ab, cudaMemcpyDeviceToHost, sd));
+        if (dl.ab) QCHK(cudaMemcpyAsync(hb + dl.vb + dl.tb + dl.ab, ainput, dl.ab, cudaMemcpyDeviceToHost, sd));
+        dl.d2h = dl.tb + 2 * dl.ab;
+    }
+    if (fork) QCHK(cudaEventRecord(ctx->ev_join, sd));
 
     // ---- Gauss-Seidel over all molecules
     if (passes > 0 && nv > 0 && T > 0) {
@@ -310,34 +355,23 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         const GsShape sh = ctx->gs_force.threads ? ctx->gs_force
                                                   : gs_shape(std::min<unsigned>(nv, 152u * kGsSlabMaxVerts), true);
         ctx->gs_used = sh;
+        // the closest-atom pass on the side stream reads the welded positions in vq
         int rc2 = run_smoothing(ctx, sh, passes, vq, pos4, nv, deg, nbr, (unsigned short *)cnt, lower, inbox,
-                                inbox_tail, d_err, nullptr, true);
+                                inbox_tail, d_err, nullptr, true, fork ? ctx->ev_join : nullptr);
         if (rc2) return rc2;
     }
     ctx->mark("smooth");
-
-    // ---- per-molecule filter and molecule-local corner ids
-    unsigned nkept = 0;
-    if (T > 0) {
-        launch_tri_flags_batch(b, tri, T, flags, s);
-        ctx->launches++;
-        QCHK(scan_u2(flags, flags, T, d_tot, tmpb, d_err, s, &ctx->launches));
-        launch_tri_compact_batch(b, tri, T, flags, tri_kept, s);
-        ctx->launches++;
-        launch_gather_offsets(flags, d_tri_off, nm, T, d_tot, d_kept_off, nullptr, s);
-        ctx->launches++;
-    } else {
-        QCHK(cudaMemsetAsync(d_kept_off, 0, 4ull * (nm + 1), s));
-        QCHK(cudaMemsetAsync(d_tot, 0, sizeof(uint2), s));
+    if (dl.want && dl.vb) {
+        QCHK(cudaMemcpyAsync(dl.block, vq, dl.vb, cudaMemcpyDeviceToHost, s));
+        dl.d2h += dl.vb;
     }
+    if (fork) QCHK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     std::vector<unsigned> kept_off(nm + 1);
-    QCHK(cudaMemcpyAsync(hsm, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
     QCHK(cudaMemcpyAsync(hsm + 2, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    QCHK(cudaMemcpyAsync(ctx->h_stage, d_kept_off, 4ull * (nm + 1), cudaMemcpyDeviceToHost, s));
     QCHK(cudaStreamSynchronize(s));
-    ctx->mark("filter");
+    ctx->mark("download");
     if (hsm[2]) return ctx->fail((int)hsm[2], "device wait in the batch mesh stage");
-    nkept = hsm[0];
+    const unsigned nkept = hsm[0];
     memcpy(kept_off.data(), ctx->h_stage, 4ull * (nm + 1));
 
     R.n_mol = nm;
