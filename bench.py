@@ -150,6 +150,7 @@ def run_gpu(args):
     voxels = float(gi.G) ** 3
     stream = torch.cuda.Stream()
     ctx = q.Context(local, stream=stream.cuda_stream)
+    ctx.set_graphs(not args.no_graphs)
     d_xyz = torch.from_numpy(xyz).cuda(local)
     d_rad = torch.from_numpy(rad).cuda(local)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -191,6 +192,7 @@ def run_gpu(args):
             torch.cuda.synchronize()
             t_wall = time.perf_counter() - t_wall0
         ms = float(np.mean(times))
+        graphs_timed = ctx.graph_stats()
     nv, nt = dm.n_vertices, dm.n_triangles
 
     # e2e through the C-ABI with host buffers (upload, pipeline, download to pinned host)
@@ -244,7 +246,8 @@ def run_gpu(args):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "smoothing_shape": None if tuned is None else
                    {"threads": tuned[0], "slab_target": tuned[1], "cache_flags": tuned[2]},
-                   "refine_tile": None if tuned is None else ("16x8" if tuned[3] == 1 else "8x8")},
+                   "refine_tile": None if tuned is None else ("16x8" if tuned[3] == 1 else "8x8"),
+                   "cuda_graphs": _graph_summary(args, graphs_timed)},
         "e2e": {"value": e2e_value, "unit": "voxels/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "qses_compute (C-ABI, pageable host atoms in, pinned host mesh out)"},
@@ -366,6 +369,15 @@ def _raw_single(lib, L, ctx, reqs):
         lib.qses_mesh_release(ctypes.byref(m))
 
 
+def _graph_summary(args, stats):
+    """How the pipeline segments ran: counters since the context was created (the
+    autotuner, warm-up and profiled calls included)."""
+    if args.no_graphs:
+        return "off (every kernel launched directly)"
+    return dict(stats, mode="segments replayed from CUDA graphs; captured again and updated in place when "
+                            "their pointers, counts or shapes change")
+
+
 def run_batch_form(args):
     """Batch form: one step = every molecule of the stream through qses_compute_batch (host
     atoms in, host meshes out).  Beside it, the same molecules one by one through
@@ -383,6 +395,7 @@ def run_batch_form(args):
     voxels = float(sum(q.grid_info(r["xyz"], r["radii"], r["voxel"]).G ** 3 for r in reqs))
     arrays, rr = A._requests(reqs)
     with q.Context(0) as ctx:
+        ctx.set_graphs(not args.no_graphs)
         tune = ctx.autotune_batch(reqs)  # launch-shape tuning, before the warm-up
         for _ in range(args.warmup):
             _raw_batch(lib, L, ctx, rr, n)
@@ -398,6 +411,7 @@ def run_batch_form(args):
                 nv, nt, bad = _raw_batch(lib, L, ctx, rr, n)
                 times.append(time.perf_counter() - t0)
         sec = float(np.mean(times))
+        graphs_timed = ctx.graph_stats()
         _raw_single(lib, L, ctx, reqs[:8])
         t0 = time.perf_counter()
         _raw_single(lib, L, ctx, reqs)
@@ -411,7 +425,8 @@ def run_batch_form(args):
         "config": {"workload": desc, "form": args.form, "molecules": n, "voxels": voxels,
                    "mesh_vertices": nv, "mesh_triangles": nt, "rejected": bad,
                    "smoothing_shape": {"threads": tune[0], "slab_target": tune[1], "cache_flags": tune[2]},
-                   "l2": "inputs and meshes far larger than L2"},
+                   "l2": "inputs and meshes far larger than L2",
+                   "cuda_graphs": _graph_summary(args, graphs_timed)},
         "voxels_per_s": voxels / sec,
         "e2e": {"value": n / sec, "unit": "molecules/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "qses_compute_batch (C-ABI, host atoms in, host meshes out)"},
@@ -504,6 +519,7 @@ def main():
     ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="served form: offered requests/s")
     ap.add_argument("--requests", type=int, default=1000, help="served form: requests per offered rate")
     ap.add_argument("--lanes", type=int, default=2, help="served form: batches in flight")
+    ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")
     ap.add_argument("--gs-shape", default="", help="profile-once: smoothing shape threads,target,cache_flags")
     ap.add_argument("--profile-once", action="store_true",
                     help="run the pipeline once on the workload (for profiler captures) and exit")

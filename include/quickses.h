@@ -245,6 +245,20 @@ QSES_API unsigned long long qses_last_download_bytes(qses_context *ctx);
  * warps).  Returns the number of values written. */
 QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max);
 
+/* ------------------------------------------------------------------ CUDA graphs */
+
+/* No reference counterpart (QuickSES launches every kernel from the host, slice by slice).
+ * A call runs as three segments between its host read-backs of counts (field, mesh, finish),
+ * each replayed from a CUDA graph kept in ctx: launched as is when the segment's pointers,
+ * counts, grid and launch shapes repeat the previous call's, captured again and updated in
+ * place otherwise.  Results are identical either way.  Segments are captured on a private
+ * stream of the context and launched on the context's stream (its own or the caller's).  On
+ * by default; with stage timing on, or enable = 0, every kernel is launched directly. */
+QSES_API int qses_set_graphs(qses_context *ctx, int enable);
+/* out[0] captures, [1] instantiations, [2] in-place updates, [3] replays, counted since the
+ * context was created.  Returns the number of values written. */
+QSES_API int qses_graph_stats(qses_context *ctx, unsigned long long *out, int max);
+
 /* ------------------------------------------------------- allocation-free field */
 
 /* No counterpart in the reference.  For callers that must not allocate GPU memory while
@@ -299,6 +313,15 @@ QSES_API int qses_grid_info_for(const qses_float3 *atoms, const float *radii, un
 QSES_API int qses_debug_codes(qses_context *ctx, uint8_t *codes, size_t bytes);
 /* Cell-sorted atom order of the last call: sorted_to_input[n], cell hash per sorted atom. */
 QSES_API int qses_debug_atom_order(qses_context *ctx, uint32_t *sorted_to_input, uint32_t *hash, unsigned n);
+/* Slab plan of the smoothing pass, for tests (no reference counterpart, no GPU needed): nv
+ * vertices, molecules' vertex ranges mol_off (nm + 1 entries; NULL = one molecule) and
+ * depth estimates, smoothing shape (threads, target, wave as qses_set_smoothing_shape) and
+ * pmax resident slab CTAs.  launch[0..5] = ctas, smax, qcap, wsize, waves, words per wave;
+ * table (cap words): the waves' slab tables [Q, Q + 1 bounds (qcap + 1 slots), Q slab ids in
+ * the order CTAs take them].  Returns QSES_OK or an error code. */
+QSES_API int qses_debug_slab_plan(unsigned nv, const unsigned *mol_off, const int *depth, unsigned nm, int threads,
+                                  unsigned target, unsigned wave, int pmax, unsigned *launch, unsigned *table,
+                                  size_t cap);
 
 /* --------------------------------------------------------- synthetic molecules */
 QSES_API int qses_synth_ball(unsigned N, uint64_t seed, float density, float min_dist, float *xyz,

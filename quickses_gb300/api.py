@@ -221,6 +221,16 @@ class Context:
     def last_launch_count(self):
         return int(self._lib.qses_last_launch_count(self._h))
 
+    def set_graphs(self, enable=True):
+        """Run the pipeline segments through CUDA graphs (default) or launch every kernel directly."""
+        self._check(self._lib.qses_set_graphs(self._h, int(bool(enable))), "qses_set_graphs")
+
+    def graph_stats(self):
+        out = (ctypes.c_ulonglong * 4)()
+        k = self._lib.qses_graph_stats(self._h, out, 4)
+        names = ["captures", "instantiations", "updates", "replays"]
+        return {names[q]: int(out[q]) for q in range(k)}
+
     def diagnostics(self):
         out = (ctypes.c_ulonglong * 10)()
         k = self._lib.qses_diagnostics(self._h, out, 10)

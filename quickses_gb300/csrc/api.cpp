@@ -39,10 +39,12 @@ class PinnedPool {
         const size_t want = size_class(bytes);
         {
             std::lock_guard<std::mutex> lock(mu_);
-            // smallest cached block that fits and wastes at most a factor 2
+            // smallest cached block that fits and wastes at most a factor 2; of equal ones the
+            // most recently returned, so a steady loop keeps downloading into the same block
+            // (and its pipeline graphs replay without a parameter update)
             size_t best = SIZE_MAX, bi = 0;
             for (size_t i = 0; i < free_.size(); i++)
-                if (free_[i].second >= want && free_[i].second <= 2 * want && free_[i].second < best) {
+                if (free_[i].second >= want && free_[i].second <= 2 * want && free_[i].second <= best) {
                     best = free_[i].second;
                     bi = i;
                 }
@@ -231,6 +233,7 @@ QSES_API int qses_context_create(int device, void *cuda_stream, qses_context **o
         ctx->own_stream = true;
     }
     if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->capture, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
@@ -253,15 +256,21 @@ QSES_API int qses_context_destroy(qses_context *ctx) {
     ctx->input.release();
     ctx->field.release();
     ctx->mesh_ws.release();
+    ctx->gs_ws.release();
+    if (ctx->h_gs) cudaFreeHost(ctx->h_gs);
     if (ctx->small) cudaFree(ctx->small);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     for (auto &m : ctx->marks) cudaEventDestroy(m.second);
+    for (auto &slot : ctx->seg)
+        for (auto &g : slot)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
     if (ctx->dl.block) qses::pinned_give(ctx->dl.block, ctx->dl.bytes);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->capture) cudaStreamDestroy(ctx->capture);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return QSES_OK;
@@ -673,6 +682,35 @@ QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int ma
     if (!ctx || !out) return 0;
     int k = 0;
     for (; k < max && k < 10; k++) out[k] = ctx->diag[k];
+    return k;
+}
+
+QSES_API int qses_debug_slab_plan(unsigned nv, const unsigned *mol_off, const int *depth, unsigned nm, int threads,
+                                  unsigned target, unsigned wave, int pmax, unsigned *launch, unsigned *table,
+                                  size_t cap) {
+    if (!launch || (nm > 1 && !mol_off)) return QSES_ERR_INVALID_ARG;
+    qses::GsPlan pl;
+    const int rc = qses::gs_plan_for(pmax, qses::GsShape{threads, target, 0, wave}, nv, mol_off, depth, nm, pl);
+    if (rc != QSES_OK) return rc;
+    const unsigned v[6] = {(unsigned)pl.L.ctas, pl.L.smax, pl.L.qcap, pl.L.wsize, pl.L.waves, pl.L.table_words};
+    memcpy(launch, v, sizeof(v));
+    if (table) {
+        if (cap < pl.table.size()) return QSES_ERR_INVALID_ARG;
+        memcpy(table, pl.table.data(), 4 * pl.table.size());
+    }
+    return QSES_OK;
+}
+
+QSES_API int qses_set_graphs(qses_context *ctx, int enable) {
+    if (!ctx) return QSES_ERR_INVALID_ARG;
+    ctx->use_graphs = enable != 0;
+    return QSES_OK;
+}
+
+QSES_API int qses_graph_stats(qses_context *ctx, unsigned long long *out, int max) {
+    if (!ctx || !out) return 0;
+    int k = 0;
+    for (; k < max && k < 4; k++) out[k] = ctx->graph_stats[k];
     return k;
 }
 

@@ -539,23 +539,33 @@ __device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
 constexpr int kGsSlabMaxSmem = 200 * 1024;  // dynamic part: offsets, packed counters, ring: 8 B/vertex
 
 // Per vertex: lower-id neighbour entries inside its slab (+1 if any lie in lower slabs),
-// and the count of entries in lower slabs.
-// Vertices [v0, v1) form the slabs.  Neighbours below v0 belong to waves that finished
-// before this one (final values); neighbours at or above v1 are read before their update.
+// the count of entries in lower slabs, and its home: slab id and the slab's first vertex.
+// Vertices [v0, v1) form the slabs of the table (Q, then Q + 1 bounds in id order).
+// Neighbours below v0 belong to waves that finished before this one (final values);
+// neighbours at or above v1 are read before their update.
 __global__ void k_gs_setup(const uint2 *__restrict__ start, const unsigned *__restrict__ nbr, unsigned v0,
-                           unsigned v1, unsigned S, unsigned short *__restrict__ cnt_local, int *__restrict__ remote) {
+                           unsigned v1, const unsigned *__restrict__ table, unsigned short *__restrict__ cnt_local,
+                           int *__restrict__ remote, uint2 *__restrict__ home) {
     unsigned v = v0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= v1) return;
-    const unsigned lo = v0 + ((v - v0) / S) * S;
+    const unsigned Q = __ldg(table);
+    const unsigned *bnd = table + 1;
+    unsigned lo = 0, hi = Q;  // bnd[lo] <= v < bnd[hi]
+    while (hi - lo > 1) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (__ldg(bnd + mid) <= v) lo = mid; else hi = mid;
+    }
+    const unsigned a = __ldg(bnd + lo);
     unsigned loc = 0, rem = 0;
     for (unsigned e = start[v].x; e < start[v + 1].x; e++) {
         const unsigned u = nbr[e];
         if (u < v && u >= v0) {  // below v0: an earlier wave, already final
-            if (u >= lo) loc++; else rem++;
+            if (u >= a) loc++; else rem++;
         }
     }
     cnt_local[v] = (unsigned short)min(loc + (rem ? 1u : 0u), 65535u);
     remote[v] = (int)rem;
+    home[v] = make_uint2(lo, a);
 }
 
 // Gauss-Seidel update of one vertex.  Positions are float4 (one 16-byte load each); the
@@ -615,27 +625,47 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
-// Warp roles: warp 0 takes boundary arrivals from lower slabs, warp 1 sends this slab's
-// cross-slab releases (GPU-scope atomics, off the workers' critical path), the other warps
-// update vertices.
+// Persistent CTAs take the wave's slabs from a counter, in the table's order (a slab only
+// waits for slabs taken before it, by CTAs that are running, so every wait ends).  Per slab,
+// warp 0 takes boundary arrivals from lower slabs, warp 1 sends this slab's cross-slab
+// releases (GPU-scope atomics, off the workers' critical path), the other warps update
+// vertices.  Table: Q, the Q + 1 slab bounds in id order (qcap + 1 slots), then the Q slab ids
+// in the order they are taken.
 template <int kGsT, unsigned kFlags>
-__global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned S,
+__global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned smax,
+                                                  const unsigned *__restrict__ table, unsigned qcap,
+                                                  unsigned *next_slab, const uint2 *__restrict__ home,
                                                   const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
                                                   const unsigned short *__restrict__ cnt_local, int *remote,
                                                   unsigned *inbox, unsigned *inbox_tail, int *err,
                                                   long long spin_cycles, unsigned long long *stats) {
     extern __shared__ unsigned s_dyn[];
-    __shared__ unsigned s_head, s_tail, s_done, s_seen, s_stop, s_ob_head, s_ob_tail;
+    __shared__ unsigned s_head, s_tail, s_done, s_stop, s_ob_head, s_ob_tail, s_slab;
     __shared__ unsigned s_ob[kGsOutbox];
-    const unsigned p = blockIdx.x, a = v0 + p * S;  // vertices [v0, nv) in slabs of S
-    if (a >= nv) return;  // uniform per CTA
-    const unsigned b = min(a + S, nv), len = b - a;
     unsigned *st = s_dyn;                                        // len + 1 CSR offsets of the slab
-    unsigned *cnt = s_dyn + (S + 1);                             // (len + 1) / 2 words: packed counters
-    volatile unsigned short *ring = (volatile unsigned short *)(cnt + (S + 1) / 2);  // slab offsets
+    unsigned *cnt = s_dyn + (smax + 1);                          // (len + 1) / 2 words: packed counters
+    volatile unsigned short *ring = (volatile unsigned short *)(cnt + (smax + 1) / 2);  // slab offsets
     volatile unsigned *ob = s_ob;
+    const unsigned Q = min(__ldg(table), qcap);
+    const unsigned *bnd = table + 1, *order = table + 2 + qcap;
+    const unsigned lane = threadIdx.x & 31;
+    unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0, cyc_ids = 0, cyc_pos = 0;
+    if (threadIdx.x == 0) s_stop = 0;
+    for (;;) {
+    if (threadIdx.x == 0) {
+        const unsigned k = atomicAdd(next_slab, 1u);
+        s_slab = (k < Q && !s_stop) ? __ldg(order + k) : 0xffffffffu;
+        s_head = 0; s_tail = 0; s_done = 0; s_ob_head = 0; s_ob_tail = 0;
+    }
+    __syncthreads();
+    const unsigned p = s_slab;
+    if (p >= Q) break;  // uniform per CTA: no slab left (or an error stopped this CTA)
+    const unsigned a = __ldg(bnd + p), b = __ldg(bnd + p + 1), len = b - a;
+    if (a < v0 || b > nv || b <= a || len > smax) {  // uniform: a malformed table entry
+        if (threadIdx.x == 0) raise_error(err, QSES_ERR_INTERNAL);
+        break;
+    }
     unsigned *box = inbox + (a - v0);                            // boundary arrivals from lower slabs
-    if (threadIdx.x == 0) { s_head = 0; s_tail = 0; s_done = 0; s_seen = 0; s_stop = 0; s_ob_head = 0; s_ob_tail = 0; }
     for (unsigned k = threadIdx.x; k < kGsOutbox; k += kGsT) s_ob[k] = 0xffffffffu;
     for (unsigned k = threadIdx.x; k <= len; k += kGsT) st[k] = start[a + k].x;
     for (unsigned k = threadIdx.x; k < len; k += kGsT) ring[k] = 0xffffu;
@@ -648,8 +678,6 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
         if (cnt_local[a + k] == 0) ring_push16(ring, &s_tail, k);
     __syncthreads();
 
-    const unsigned lane = threadIdx.x & 31;
-    unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0, cyc_ids = 0, cyc_pos = 0;
     if (threadIdx.x < 32) {
         // Warp 0 only takes boundary arrivals (the last lower-slab dependency of a vertex
         // finished); it never updates vertices, so arrivals are never stuck behind a chain.
@@ -711,11 +739,11 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
                 } else {
                     *slot = 0xffffffffu;
                     __threadfence_block();
+                    const uint2 h = __ldg(home + u);  // u's slab and its first vertex (constant)
                     if (atom_sub_acq_rel(remote + u, 1) == 1) {
                         // last lower-slab dependency of u: hand u to its slab
-                        const unsigned qs = (u - v0) / S;
-                        const unsigned k = atomicAdd(inbox_tail + qs, 1u);
-                        if (k < S) st_release_u32(inbox + (size_t)qs * S + k, u);
+                        const unsigned k = atomicAdd(inbox_tail + h.x, 1u);
+                        if (k < smax && h.x < Q) st_release_u32(inbox + (h.y - v0) + k, u);
                     }
                 }
             }
@@ -857,11 +885,10 @@ __global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, 
         }
     }
     __syncthreads();
-    if (stats) {  // diagnostics: polls (max), unfinished slabs, update cycles, release cycles, vertices
-        if (threadIdx.x == 0) {
-            atomicMax(stats, polls);
-            if (s_done < len) atomicAdd(stats + 1, 1ull);
-        }
+    if (stats && threadIdx.x == 0 && s_done < len) atomicAdd(stats + 1, 1ull);  // unfinished slabs
+    }  // next slab
+    if (stats) {  // diagnostics: polls (max), update cycles, release cycles, vertices
+        if (threadIdx.x == 0) atomicMax(stats, polls);
         if (lane == 0 && nproc) {
             atomicAdd(stats + 2, cyc_update);
             atomicAdd(stats + 3, cyc_release);
@@ -952,9 +979,9 @@ void launch_copy_keys(const unsigned *tri, size_t n3, unsigned *keys, cudaStream
 void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s) {
     k_csr_fill<<<nblk(n3, 256), 256, 0, s>>>(tri, socc, n3, nbr);
 }
-void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, unsigned S,
-                     unsigned short *cnt_local, int *remote, cudaStream_t s) {
-    k_gs_setup<<<nblk(v1 - v0, 256), 256, 0, s>>>(start, nbr, v0, v1, S, cnt_local, remote);
+void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, const unsigned *table,
+                     unsigned short *cnt_local, int *remote, uint2 *home, cudaStream_t s) {
+    k_gs_setup<<<nblk(v1 - v0, 256), 256, 0, s>>>(start, nbr, v0, v1, table, cnt_local, remote, home);
 }
 size_t gs_slab_smem(unsigned S) { return 4ull * (S + 1) + 4ull * ((S + 1) / 2) + 2ull * S + 16; }
 void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s) {
@@ -971,14 +998,17 @@ static const void *gs_flow_fn(int threads, unsigned flags) {
          (const void *)k_gs_flow<1024, 3>}};
     return fn[threads >= 1024 ? 1 : 0][flags & 3u];
 }
-cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads, unsigned flags,
+cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax, const unsigned *table,
+                           unsigned qcap, unsigned *next_slab, const uint2 *home, int P, int threads, unsigned flags,
                            const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
                            unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
                            unsigned long long *stats, cudaStream_t s) {
-    size_t smem = gs_slab_smem(S);
+    if (smax == 0 || smax > kGsSlabMaxVerts) return cudaErrorInvalidValue;
+    size_t smem = gs_slab_smem(smax);
     const void *fn = gs_flow_fn(threads, flags);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
-    void *args[] = {&pos, &v0, &nv, &S, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
+    void *args[] = {&pos,    &v0,    &nv,          &smax,  (void *)&table, &qcap,         &next_slab,
+                    (void *)&home, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
                     &inbox_tail, &err, &spin_cycles, &stats};
     return cudaLaunchCooperativeKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
 }

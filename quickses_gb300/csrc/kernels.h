@@ -31,14 +31,19 @@ void launch_tri_compact(const unsigned *tri, unsigned nt, const uint2 *excl, uns
 void launch_degree(const unsigned *tri, size_t n3, unsigned nv, uint2 *deg, cudaStream_t s);
 void launch_copy_keys(const unsigned *tri, size_t n3, unsigned *keys, cudaStream_t s);
 void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s);
-void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, unsigned S,
-                     unsigned short *cnt_local, int *remote, cudaStream_t s);
+// Slab table of one Gauss-Seidel wave (device words): [0] Q slabs, [1, Q + 2) their bounds in
+// id order (qcap + 1 slots), [qcap + 2, qcap + 2 + Q) the slab ids in the order CTAs take them.
+inline size_t gs_table_words(unsigned qcap) { return 2ull * qcap + 2; }
+void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, const unsigned *table,
+                     unsigned short *cnt_local, int *remote, uint2 *home, cudaStream_t s);
 size_t gs_slab_smem(unsigned S);
 void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s);
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s);
-// One Gauss-Seidel pass over vertices [v0, nv) in P slabs of S (no neighbour outside).
-// threads: 512 or 1024 per slab CTA.
-cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned S, int P, int threads, unsigned flags,
+// One Gauss-Seidel pass over vertices [v0, nv) in the table's slabs (each at most smax
+// vertices), taken by P persistent CTAs from *next_slab (zeroed, like inbox_tail's qcap
+// counters).  threads: 512 or 1024 per slab CTA.
+cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax, const unsigned *table,
+                           unsigned qcap, unsigned *next_slab, const uint2 *home, int P, int threads, unsigned flags,
                            const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
                            unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
                            unsigned long long *stats, cudaStream_t s);

@@ -16,6 +16,7 @@
 #include "kernels.h"
 #include "prims.h"
 #include "qses_context.h"
+#include "segment.h"
 
 namespace qses {
 
@@ -151,7 +152,10 @@ void edt_shape_record(int G, int shape) {
 
 int gs_shape_candidates(GsShape *out, int max) {
     static const unsigned targets[] = {4096, 16384, 25000};
-    static const unsigned flags[] = {0, kGsL1Positions, kGsPersistL2, kGsPersistL2 | kGsL1Positions};
+    // the persisting-L2 window (kGsPersistL2) is left to callers that force it: it changes
+    // stream attributes (its segment then runs outside CUDA graphs) and its reset after the
+    // pass costs more than the pass gains
+    static const unsigned flags[] = {0, kGsL1Positions, kGsL1Prefetch, kGsL1Prefetch | kGsL1Positions};
     int k = 0;
     for (int t : {512, 1024})
         for (unsigned tg : targets)
@@ -199,50 +203,358 @@ void Arena::release() {
         if (e_ != cudaSuccess) return ctx->fail(QSES_ERR_CUDA, #expr, e_);              \
     } while (0)
 
+#define QCHK_RC(expr)                                                                   \
+    do {                                                                                \
+        const int rc_ = (expr);                                                         \
+        if (rc_ != QSES_OK) return rc_;                                                 \
+    } while (0)
+
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-int run_smoothing(qses_context *ctx, const GsShape &sh, int passes, float *vq, float4 *pos4, unsigned nv,
-                  const uint2 *deg, const unsigned *nbr, unsigned short *cnt, int *remote, unsigned *inbox,
-                  unsigned *inbox_tail, int *d_err, unsigned long long *stats, bool record_slabs,
-                  cudaEvent_t before_writeback) {
+static unsigned ceil_div(unsigned long long a, unsigned long long b) { return (unsigned)((a + b - 1) / b); }
+
+int gs_plan(int device, const GsShape &sh, unsigned nv, const unsigned *mol_off, const int *mol_depth, unsigned nm,
+            GsPlan &pl) {
+    const int pmax = std::min(gs_slab_max_blocks(device, kGsSlabMaxVerts, sh.threads), 1024);
+    if (pmax < 1) return QSES_ERR_NO_DEVICE;
+    return gs_plan_for(pmax, sh, nv, mol_off, mol_depth, nm, pl);
+}
+
+int gs_plan_for(int pmax, const GsShape &sh, unsigned nv, const unsigned *mol_off, const int *mol_depth, unsigned nm,
+                GsPlan &pl) {
+    pl = GsPlan();
+    if (pmax < 1 || nv == 0) return QSES_ERR_INVALID_ARG;
+    const unsigned Smax = kGsSlabMaxVerts;
+    const unsigned t = std::min(std::max(sh.target, 256u), Smax);
+    const bool single = mol_off == nullptr || nm <= 1;
+    const unsigned cap = sh.wave ? std::max(sh.wave, 1u) : nv;
+    GsLaunch &L = pl.L;
+    L.waves = ceil_div(nv, cap);
+    L.wsize = ceil_div(nv, L.waves);  // balanced waves
+    // slabs of one molecule of len vertices: spread over at most pmax CTAs, at least t per slab,
+    // at most Smax per slab
+    auto pieces = [&](unsigned len) {
+        return std::max(ceil_div(len, Smax), std::min(ceil_div(len, t), (unsigned)pmax));
+    };
+    if (single) {
+        L.qcap = pieces(L.wsize);
+        L.smax = 0;
+        for (unsigned w = 0; w < L.waves; w++) {
+            const unsigned nw = std::min(nv, (w + 1) * L.wsize) - w * L.wsize;
+            L.smax = std::max(L.smax, ceil_div(nw, pieces(nw)));
+            L.qcap = std::max(L.qcap, pieces(nw));
+        }
+    } else {
+        // split molecules: at most len / t + 1 slabs each; packed runs of small molecules: at most
+        // 2 (run / t) + 1 (two neighbouring packed slabs hold more than t)
+        L.qcap = 2 * ceil_div(L.wsize, t) + 2 * nm + 2;
+        L.smax = Smax;
+    }
+    L.ctas = (int)std::min<unsigned>((unsigned)pmax, L.qcap);
+    L.table_words = (unsigned)gs_table_words(L.qcap);
+    pl.table.assign((size_t)L.waves * L.table_words, 0u);
+
+    struct Slab {
+        unsigned a, b;
+        float when;  // expected start: fraction of the molecule before the slab x its depth
+        int depth;
+    };
+    std::vector<Slab> slabs;
+    std::vector<unsigned> ord;
+    for (unsigned w = 0; w < L.waves; w++) {
+        const unsigned v0 = w * L.wsize, v1 = std::min(nv, v0 + L.wsize);
+        slabs.clear();
+        auto split = [&](unsigned s0, unsigned s1, int depth) {
+            const unsigned len = s1 - s0, k = pieces(len), S = ceil_div(len, k);
+            for (unsigned a = s0; a < s1; a += S)
+                slabs.push_back({a, std::min(s1, a + S), (float)((double)(a - s0) / len * depth), depth});
+        };
+        if (single) {
+            split(v0, v1, 1);
+        } else {
+            unsigned pa = 0, pb = 0;  // pending packed slab [pa, pb)
+            auto flush = [&]() {
+                if (pb > pa) slabs.push_back({pa, pb, 0.0f, 0});
+                pa = pb = 0;
+            };
+            for (unsigned m = 0; m < nm; m++) {
+                const unsigned s0 = std::max(mol_off[m], v0), s1 = std::min(mol_off[m + 1], v1);
+                if (s1 <= s0) continue;
+                const unsigned len = s1 - s0;
+                if (len > t) {
+                    flush();
+                    split(s0, s1, mol_depth ? std::max(mol_depth[m], 1) : 1);
+                } else {
+                    if (pb > pa && (pb - pa) + len > t) flush();
+                    if (pb == pa) pa = s0;
+                    pb = s1;
+                }
+            }
+            flush();
+        }
+        const unsigned Q = (unsigned)slabs.size();
+        if (Q == 0 || Q > L.qcap || slabs.front().a != v0 || slabs.back().b != v1) return QSES_ERR_INTERNAL;
+        unsigned *tb = pl.table.data() + (size_t)w * L.table_words;
+        tb[0] = Q;
+        for (unsigned q = 0; q < Q; q++) {
+            if (slabs[q].b - slabs[q].a > L.smax || (q && slabs[q].a != slabs[q - 1].b)) return QSES_ERR_INTERNAL;
+            tb[1 + q] = slabs[q].a;
+            pl.max_len = std::max(pl.max_len, slabs[q].b - slabs[q].a);
+        }
+        tb[1 + Q] = v1;
+        // CTAs take slabs in order of expected start (ties: deeper molecule, then id).  Within a
+        // molecule the expected start grows with the id, so a slab is always taken after the
+        // lower slabs it waits for.
+        ord.resize(Q);
+        for (unsigned q = 0; q < Q; q++) ord[q] = q;
+        std::sort(ord.begin(), ord.end(), [&](unsigned x, unsigned y) {
+            if (slabs[x].when != slabs[y].when) return slabs[x].when < slabs[y].when;
+            if (slabs[x].depth != slabs[y].depth) return slabs[x].depth > slabs[y].depth;
+            return x < y;
+        });
+        for (unsigned q = 0; q < Q; q++) tb[2 + L.qcap + q] = ord[q];
+        pl.max_slabs = std::max(pl.max_slabs, Q);
+    }
+    return QSES_OK;
+}
+
+int gs_buffers(qses_context *ctx, const GsPlan &pl, unsigned nv, GsBuffers &out) {
+    const GsLaunch &L = pl.L;
+    const size_t words = pl.table.size();
+    const size_t need = align256(8ull * nv + 8) + align256(4 * words) + align256(4ull * (L.wsize + L.smax + 64)) +
+                        align256(4ull * (L.qcap + 2)) + 4096;
+    if (ctx->gs_ws.reserve(need) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "smoothing workspace");
+    out.home = (uint2 *)ctx->gs_ws.take(8ull * nv + 8);
+    out.table = (unsigned *)ctx->gs_ws.take(4 * words);
+    out.inbox = (unsigned *)ctx->gs_ws.take(4ull * (L.wsize + L.smax + 64));
+    out.inbox_tail = (unsigned *)ctx->gs_ws.take(4ull * (L.qcap + 2));  // per slab, then the slab counter
+    if (!out.inbox_tail) return ctx->fail(QSES_ERR_INTERNAL, "smoothing workspace layout");
+    if (4 * words > ctx->h_gs_cap) {
+        if (ctx->h_gs) cudaFreeHost(ctx->h_gs);
+        ctx->h_gs = nullptr;
+        ctx->h_gs_cap = 0;
+        const size_t want = 4 * words + 2 * words + 4096;
+        if (cudaMallocHost((void **)&ctx->h_gs, want) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->h_gs = nullptr;
+            return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned slab tables");
+        }
+        ctx->h_gs_cap = want;
+    }
+    memcpy(ctx->h_gs, pl.table.data(), 4 * words);
+    return QSES_OK;
+}
+
+int run_smoothing(qses_context *ctx, const GsShape &sh, const GsLaunch &L, int passes, float *vq, float4 *pos4,
+                  unsigned nv, const uint2 *deg, const unsigned *nbr, unsigned short *cnt, int *remote, uint2 *home,
+                  unsigned *table, const unsigned *h_table, unsigned *inbox, unsigned *inbox_tail, int *d_err,
+                  unsigned long long *stats, cudaEvent_t before_writeback) {
     cudaStream_t s = ctx->stream;
-    const int pmax = std::min(gs_slab_max_blocks(ctx->device, kGsSlabMaxVerts, sh.threads), 1024);
-    if (pmax < 1) return ctx->fail(QSES_ERR_NO_DEVICE, "the smoothing kernel does not fit on this device");
-    unsigned long long cap = (unsigned long long)pmax * kGsSlabMaxVerts;
-    if (sh.wave && sh.wave < cap) cap = sh.wave;
-    const unsigned nwaves = (unsigned)((nv + cap - 1) / cap);
-    const unsigned wsize = (nv + nwaves - 1) / nwaves;  // balanced waves
     launch_to_float4(vq, nv, pos4, s);
     ctx->launches++;
     if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, pos4, 16ull * nv);
     if (stats) QCHK(cudaMemsetAsync(stats, 0, 64, s));
+    QCHK(cudaMemcpyAsync(table, h_table, 4ull * L.waves * L.table_words, cudaMemcpyHostToDevice, s));
     for (int pass = 0; pass < passes; pass++) {
-        for (unsigned v0 = 0; v0 < nv; v0 += wsize) {
-            const unsigned v1 = std::min(nv, v0 + wsize), nw = v1 - v0;
-            int P = (int)std::min<unsigned>((nw + sh.target - 1) / sh.target, (unsigned)pmax);
-            if (P < 1) P = 1;
-            unsigned S = (nw + P - 1) / P;
-            if (S > kGsSlabMaxVerts) {
-                P = (int)((nw + kGsSlabMaxVerts - 1) / kGsSlabMaxVerts);
-                S = (nw + P - 1) / P;
-            }
-            launch_gs_setup(deg, nbr, v0, v1, S, cnt, remote, s);
+        for (unsigned w = 0; w < L.waves; w++) {
+            const unsigned v0 = w * L.wsize, v1 = std::min(nv, v0 + L.wsize);
+            const unsigned *tb = table + (size_t)w * L.table_words;
+            launch_gs_setup(deg, nbr, v0, v1, tb, cnt, remote, home, s);
             ctx->launches++;
-            QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * P * S, s));
-            QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * P, s));
-            QCHK(launch_gs_slab(pos4, v0, v1, S, P, sh.threads, sh.flags, deg, nbr, cnt, remote, inbox, inbox_tail,
-                                d_err, 4000000000ll, stats, s));
+            QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * (v1 - v0), s));
+            QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * (L.qcap + 1), s));
+            QCHK(launch_gs_slab(pos4, v0, v1, L.smax, tb, L.qcap, inbox_tail + L.qcap, home, L.ctas, sh.threads,
+                                sh.flags, deg, nbr, cnt, remote, inbox, inbox_tail, d_err, 4000000000ll, stats, s));
             ctx->launches++;
-            if (record_slabs) {
-                ctx->diag[0] = std::max<unsigned long long>(ctx->diag[0], (unsigned long long)P);
-                ctx->diag[1] = std::max<unsigned long long>(ctx->diag[1], (unsigned long long)S);
-            }
         }
     }
     if (sh.flags & kGsPersistL2) gs_l2_window(ctx->device, s, nullptr, 0);
     if (before_writeback) QCHK(cudaStreamWaitEvent(s, before_writeback, 0));
     launch_from_float4(pos4, nv, vq, s);
     ctx->launches++;
+    return QSES_OK;
+}
+
+// ---- segment 1: atoms sorted into cells, SES field codes, marching-cubes row counts
+struct FieldSeg {
+    const float *xyz, *r;
+    unsigned *key, *key2, *idx, *idx2;
+    float4 *atoms;
+    uint2 *cells;
+    unsigned *in_mask, *out_mask, *sign_mask;
+    unsigned char *codes;
+    float *lut;
+    const unsigned char *h_lut;  // pinned; the copy node reads it when the segment runs
+    uint2 *rows, *tot;
+    void *tmp;
+    int *err;
+    unsigned char *h_out;  // pinned: [0, 8) totals, [8, 12) error word
+    unsigned long long ncell, nrow;
+    unsigned n;
+    int atom_bits, edt, pad_;
+    QGrid g;
+};
+
+static int enqueue_field(qses_context *ctx, const FieldSeg &a, SegOut &o) {
+    cudaStream_t s = ctx->stream;
+    QCHK(cudaMemcpyAsync(a.lut, a.h_lut, 1024, cudaMemcpyHostToDevice, s));
+    launch_atom_hash(a.g, a.xyz, a.n, a.key, s);
+    ctx->launches++;
+    QCHK(radix_sort<unsigned>(a.key, a.key2, a.idx, a.idx2, a.n, a.atom_bits, true, a.tmp, a.err, s, &ctx->launches,
+                              &o.alt));
+    const unsigned *skey = o.alt ? a.key2 : a.key, *sidx = o.alt ? a.idx2 : a.idx;
+    QCHK(cudaMemsetAsync(a.cells, 0, 8 * a.ncell, s));
+    launch_atom_gather(a.xyz, a.r, skey, sidx, a.n, a.atoms, a.cells, s);
+    ctx->launches++;
+    ctx->mark("atoms");
+    launch_sas(a.g, a.atoms, a.cells, a.in_mask, a.out_mask, s);
+    ctx->launches++;
+    ctx->mark("sas");
+    launch_edt(a.g, a.in_mask, a.out_mask, a.codes, a.sign_mask, s, a.edt);
+    ctx->launches++;
+    ctx->mark("refine");
+    launch_mc_count(a.g, a.sign_mask, a.rows, s);
+    ctx->launches++;
+    QCHK(scan_u2(a.rows, a.rows, (unsigned)a.nrow, a.tot, a.tmp, a.err, s, &ctx->launches));
+    QCHK(cudaMemcpyAsync(a.h_out, a.tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    QCHK(cudaMemcpyAsync(a.h_out + 8, a.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return QSES_OK;
+}
+
+// ---- segment 2: triangles and pre-weld vertex keys, weld (sort, unique, rank, remap)
+struct MeshSeg {
+    const unsigned *sign_mask;
+    const unsigned char *codes;
+    const float *lut;
+    const uint2 *rows;
+    unsigned *tri;
+    unsigned long long *vk, *vk2;
+    unsigned *vv, *vv2;
+    uint2 *flags, *tot;
+    unsigned *vmap;
+    float *vq;
+    void *tmp;
+    int *err;
+    unsigned char *h_out;  // pinned: [0, 8) vertex total
+    unsigned long long n3;
+    unsigned ne;
+    int key_bits;
+    QGrid g;
+};
+
+static int enqueue_mesh(qses_context *ctx, const MeshSeg &b, SegOut &o) {
+    cudaStream_t s = ctx->stream;
+    launch_mc_emit(b.g, b.sign_mask, b.codes, b.lut, b.rows, b.tri, b.vk, s);
+    ctx->launches++;
+    ctx->mark("mc_emit");
+    if (b.ne > 0) {
+        QCHK(radix_sort<unsigned long long>(b.vk, b.vk2, b.vv, b.vv2, b.ne, b.key_bits, true, b.tmp, b.err, s,
+                                            &ctx->launches, &o.alt));
+        const unsigned long long *sk = o.alt ? b.vk2 : b.vk;
+        const unsigned *sv = o.alt ? b.vv2 : b.vv;
+        launch_weld_flags(sk, b.ne, b.flags, s);
+        ctx->launches++;
+        QCHK(scan_u2(b.flags, b.flags, b.ne, b.tot, b.tmp, b.err, s, &ctx->launches));
+        launch_weld_scatter(b.g, sk, sv, b.flags, b.ne, b.vmap, b.vq, s);
+        ctx->launches++;
+        launch_remap(b.tri, b.n3, b.vmap, s);
+        ctx->launches++;
+        QCHK(cudaMemcpyAsync(b.h_out, b.tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    }
+    return QSES_OK;
+}
+
+// ---- segment 3: closest atom, degenerate filter and host downloads on the side stream;
+// neighbour lists and Gauss-Seidel on the main stream; final read-backs
+struct FinishSeg {
+    const float4 *atoms;
+    const uint2 *cells;
+    const unsigned *sidx;
+    int *asorted, *ainput;
+    float *vq;
+    unsigned *tri, *tri_kept;
+    uint2 *tflags;
+    void *tmp2;
+    uint2 *tot;
+    int *err;
+    unsigned char *h_out;  // pinned: [0, 8) kept triangles, [8, 12) error word, [2048, 2112) stats
+    char *h_dl;            // pinned host mesh block, or null
+    unsigned long long dl_vb, dl_tb, dl_ab;
+    uint2 *deg;
+    unsigned *okey, *okey2, *oval, *oval2, *nbr;
+    void *tmpb;
+    float4 *pos4;
+    unsigned short *cnt;
+    int *lower;
+    uint2 *home;
+    unsigned *table;
+    const unsigned *h_table;  // pinned slab tables; the copy node reads them when the segment runs
+    unsigned *inbox, *inbox_tail;
+    unsigned long long *stats;
+    unsigned long long n3;
+    unsigned nv, nt;
+    int passes, keep_all, fork, pad_;
+    GsShape sh;
+    GsLaunch gl;
+    QGrid g;
+};
+
+static int enqueue_finish(qses_context *ctx, const FinishSeg &c, SegOut &o) {
+    cudaStream_t s = ctx->stream, sd = c.fork ? ctx->side : s;
+    if (c.fork) {
+        QCHK(cudaEventRecord(ctx->ev_fork, s));
+        QCHK(cudaStreamWaitEvent(sd, ctx->ev_fork, 0));
+    }
+    // closest atom per welded vertex (before smoothing, as in the reference)
+    if (c.nv > 0) {
+        launch_closest(c.g, c.vq, c.nv, c.atoms, c.cells, c.sidx, c.asorted, c.ainput, sd);
+        ctx->launches++;
+    }
+    ctx->mark("closest_atom");
+    // drop degenerate triangles (API_computeSES filter)
+    if (!c.keep_all && c.nt > 0) {
+        launch_tri_flags(c.tri, c.nt, c.tflags, sd);
+        ctx->launches++;
+        QCHK(scan_u2(c.tflags, c.tflags, c.nt, c.tot, c.tmp2, c.err, sd, &ctx->launches));
+        launch_tri_compact(c.tri, c.nt, c.tflags, c.tri_kept, sd);
+        ctx->launches++;
+        QCHK(cudaMemcpyAsync(c.h_out, c.tot, sizeof(uint2), cudaMemcpyDeviceToHost, sd));
+    }
+    ctx->mark("filter");
+    const unsigned *tri_out = c.keep_all ? c.tri : c.tri_kept;
+    if (c.h_dl) {
+        if (c.dl_tb) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb, tri_out, c.dl_tb, cudaMemcpyDeviceToHost, sd));
+        if (c.dl_ab) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb, c.asorted, c.dl_ab, cudaMemcpyDeviceToHost, sd));
+        if (c.dl_ab)
+            QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb + c.dl_ab, c.ainput, c.dl_ab, cudaMemcpyDeviceToHost, sd));
+    }
+    if (c.fork) QCHK(cudaEventRecord(ctx->ev_join, sd));
+
+    // Gauss-Seidel smoothing on the device
+    if (c.passes > 0 && c.nv > 0 && c.nt > 0) {
+        QCHK(cudaMemsetAsync(c.deg, 0, 8ull * (c.nv + 1), s));
+        launch_degree(c.tri, c.n3, c.nv, c.deg, s);
+        ctx->launches++;
+        QCHK(scan_u2(c.deg, c.deg, c.nv + 1, nullptr, c.tmpb, c.err, s, &ctx->launches));
+        launch_copy_keys(c.tri, c.n3, c.okey, s);
+        ctx->launches++;
+        QCHK(radix_sort<unsigned>(c.okey, c.okey2, c.oval, c.oval2, (unsigned)c.n3, bits_for(c.nv - 1), true, c.tmpb,
+                                  c.err, s, &ctx->launches, &o.alt));
+        const unsigned *socc = o.alt ? c.oval2 : c.oval;
+        launch_csr_fill(c.tri, socc, c.n3, c.nbr, s);
+        ctx->launches++;
+        ctx->mark("smooth_csr");
+        // the closest-atom pass on the side stream reads the welded positions in vq
+        const int rc = run_smoothing(ctx, c.sh, c.gl, c.passes, c.vq, c.pos4, c.nv, c.deg, c.nbr, c.cnt, c.lower,
+                                     c.home, c.table, c.h_table, c.inbox, c.inbox_tail, c.err, c.stats,
+                                     c.fork ? ctx->ev_join : nullptr);
+        if (rc) return rc;
+    }
+    ctx->mark("smooth");
+    if (c.h_dl && c.dl_vb) QCHK(cudaMemcpyAsync(c.h_dl, c.vq, c.dl_vb, cudaMemcpyDeviceToHost, s));
+    if (c.fork) QCHK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    QCHK(cudaMemcpyAsync(c.h_out + 8, c.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    QCHK(cudaMemcpyAsync(c.h_out + 2048, c.stats, 64, cudaMemcpyDeviceToHost, s));
     return QSES_OK;
 }
 
@@ -295,48 +607,39 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
                    align256(ncode) + align256(1024) + 2 * align256(8 * nrow) + align256(tmpA) + 4096;
     if (ctx->field.reserve(needA) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "field workspace");
     Arena &A = ctx->field;
-    unsigned *key = (unsigned *)A.take(4ull * n), *key2 = (unsigned *)A.take(4ull * n);
-    unsigned *idx = (unsigned *)A.take(4ull * n), *idx2 = (unsigned *)A.take(4ull * n);
-    float4 *atoms = (float4 *)A.take(16ull * n);
-    uint2 *cells = (uint2 *)A.take(8 * ncell);
-    unsigned *inMask = (unsigned *)A.take(4 * nmask), *outMask = (unsigned *)A.take(4 * nmask);
-    unsigned *signMask = (unsigned *)A.take(4 * nmask);
-    unsigned char *codes = (unsigned char *)A.take(ncode);
-    float *d_lut = (float *)A.take(1024);
-    uint2 *rows = (uint2 *)A.take(8 * nrow);
-    uint2 *d_tot = (uint2 *)A.take(64);
-    void *tmp = A.take(tmpA);
-    float h_lut[256];
-    fill_lut(g, h_lut);
-    memcpy(ctx->h_small + 64, h_lut, sizeof(h_lut));
-    QCHK(cudaMemcpyAsync(d_lut, ctx->h_small + 64, sizeof(h_lut), cudaMemcpyHostToDevice, s));
-
-    // ---- atoms: cell keys, stable radix sort, sorted xyzr + cell ranges
-    launch_atom_hash(g, d_xyz, n, key, s);
-    ctx->launches++;
-    int alt = 0;
-    QCHK(radix_sort<unsigned>(key, key2, idx, idx2, n, atom_bits, true, tmp, d_err, s, &ctx->launches, &alt));
-    unsigned *skey = alt ? key2 : key, *sidx = alt ? idx2 : idx;
-    QCHK(cudaMemsetAsync(cells, 0, 8 * ncell, s));
-    launch_atom_gather(d_xyz, d_r, skey, sidx, n, atoms, cells, s);
-    ctx->launches++;
-    ctx->mark("atoms");
-
-    // ---- SES field
-    launch_sas(g, atoms, cells, inMask, outMask, s);
-    ctx->launches++;
-    ctx->mark("sas");
+    FieldSeg a;
+    memset(&a, 0, sizeof(a));
+    a.xyz = d_xyz;
+    a.r = d_r;
+    a.key = (unsigned *)A.take(4ull * n);
+    a.key2 = (unsigned *)A.take(4ull * n);
+    a.idx = (unsigned *)A.take(4ull * n);
+    a.idx2 = (unsigned *)A.take(4ull * n);
+    a.atoms = (float4 *)A.take(16ull * n);
+    a.cells = (uint2 *)A.take(8 * ncell);
+    a.in_mask = (unsigned *)A.take(4 * nmask);
+    a.out_mask = (unsigned *)A.take(4 * nmask);
+    a.sign_mask = (unsigned *)A.take(4 * nmask);
+    a.codes = (unsigned char *)A.take(ncode);
+    a.lut = (float *)A.take(1024);
+    a.rows = (uint2 *)A.take(8 * nrow);
+    a.tot = (uint2 *)A.take(64);
+    a.tmp = A.take(tmpA);
+    a.err = d_err;
+    a.h_lut = ctx->h_small + 64;
+    a.h_out = ctx->h_small;
+    a.ncell = ncell;
+    a.nrow = nrow;
+    a.n = n;
+    a.atom_bits = atom_bits;
     ctx->edt_used = ctx->edt_force >= 0 ? ctx->edt_force : edt_shape(g.G);
-    launch_edt(g, inMask, outMask, codes, signMask, s, ctx->edt_used);
-    ctx->launches++;
-    ctx->mark("refine");
-
-    // ---- marching cubes: per-row counts, scan, totals
-    launch_mc_count(g, signMask, rows, s);
-    ctx->launches++;
-    QCHK(scan_u2(rows, rows, (unsigned)nrow, d_tot, tmp, d_err, s, &ctx->launches));
-    QCHK(cudaMemcpyAsync(ctx->h_small, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
-    QCHK(cudaMemcpyAsync(ctx->h_small + 8, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    a.edt = ctx->edt_used;
+    a.g = g;
+    if (!a.tmp) return ctx->fail(QSES_ERR_INTERNAL, "field workspace layout");
+    fill_lut(g, (float *)(ctx->h_small + 64));
+    SegOut oa;
+    QCHK_RC(run_segment(ctx, kSegField, a, oa, enqueue_field));
+    unsigned *skey = oa.alt ? a.key2 : a.key, *sidx = oa.alt ? a.idx2 : a.idx;
     QCHK(cudaStreamSynchronize(s));
     ctx->mark("mc_count");
     uint2 tot;
@@ -357,7 +660,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     const size_t nflag = std::max<size_t>((size_t)NE + 1, (size_t)T) + 1;
     size_t needB = 2 * align256(4 * n3) + 2 * align256(8ull * NE) + 2 * align256(4ull * NE) + align256(8ull * nflag) +
                    align256(4ull * NE) + align256(12ull * NE) + 2 * align256(4ull * NE) + 2 * align256(4 * n3) +
-                   2 * align256(4 * n3) + align256(8 * n3) + 3 * align256(4ull * NE) + align256(4ull * NE + 4096) + 4096 +
+                   2 * align256(4 * n3) + align256(8 * n3) + 3 * align256(4ull * NE) + 4096 +
                    align256(16ull * NE + 16) +
                    align256(tmpB) + align256(8ull * T + 16) + align256(scan_u2_tmp_bytes(T + 1)) + 4096;
     if (ctx->mesh_ws.reserve(needB) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "mesh workspace");
@@ -374,33 +677,39 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     unsigned *oval = (unsigned *)B.take(4 * n3 + 4), *oval2 = (unsigned *)B.take(4 * n3 + 4);
     unsigned *nbr = (unsigned *)B.take(8 * n3 + 8);
     int *lower = (int *)B.take(4ull * NE + 4), *cnt = (int *)B.take(4ull * NE + 4);
-    unsigned *inbox = (unsigned *)B.take(4ull * NE + 4096);
-    unsigned *inbox_tail = (unsigned *)B.take(4096);
     float4 *pos4 = (float4 *)B.take(16ull * NE + 16);
     void *tmpb = B.take(tmpB);
     uint2 *tflags = (uint2 *)B.take(8ull * T + 16);      // degenerate filter (side stream)
     void *tmp2 = B.take(scan_u2_tmp_bytes(T + 1));       // its scan's scratch
     if (!tmpb || !tflags || !tmp2) return ctx->fail(QSES_ERR_INTERNAL, "mesh workspace layout");
 
-    // ---- triangles + pre-weld vertex keys
-    launch_mc_emit(g, signMask, codes, d_lut, rows, tri, vk, s);
-    ctx->launches++;
-    ctx->mark("mc_emit");
-
-    // ---- weld: sort keys, unique, rank, remap triangle corners
+    // ---- triangles + pre-weld vertex keys; weld
+    MeshSeg b;
+    memset(&b, 0, sizeof(b));
+    b.sign_mask = a.sign_mask;
+    b.codes = a.codes;
+    b.lut = a.lut;
+    b.rows = a.rows;
+    b.tri = tri;
+    b.vk = vk;
+    b.vk2 = vk2;
+    b.vv = vv;
+    b.vv2 = vv2;
+    b.flags = flags;
+    b.tot = a.tot;
+    b.vmap = vmap;
+    b.vq = vq;
+    b.tmp = tmpb;
+    b.err = d_err;
+    b.h_out = ctx->h_small;
+    b.n3 = n3;
+    b.ne = NE;
+    b.key_bits = key_bits;
+    b.g = g;
+    SegOut ob;
+    QCHK_RC(run_segment(ctx, kSegMesh, b, ob, enqueue_mesh));
     unsigned nv = 0;
     if (NE > 0) {
-        QCHK(radix_sort<unsigned long long>(vk, vk2, vv, vv2, NE, key_bits, true, tmpb, d_err, s, &ctx->launches, &alt));
-        unsigned long long *sk = alt ? vk2 : vk;
-        unsigned *sv = alt ? vv2 : vv;
-        launch_weld_flags(sk, NE, flags, s);
-        ctx->launches++;
-        QCHK(scan_u2(flags, flags, NE, d_tot, tmpb, d_err, s, &ctx->launches));
-        launch_weld_scatter(g, sk, sv, flags, NE, vmap, vq, s);
-        ctx->launches++;
-        launch_remap(tri, n3, vmap, s);
-        ctx->launches++;
-        QCHK(cudaMemcpyAsync(ctx->h_small, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
         QCHK(cudaStreamSynchronize(s));
         memcpy(&tot, ctx->h_small, sizeof(tot));
         nv = tot.x;
@@ -410,8 +719,6 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     // Closest atom, degenerate filter and (for host results) the triangle and atom-id
     // downloads run on the side stream while the main stream builds the neighbour lists and
     // smooths; profiled calls keep one stream so the stage times stay separable.
-    const bool fork = !ctx->profiling && ctx->side != nullptr;
-    cudaStream_t sd = fork ? ctx->side : s;
     const bool keep_all = (p.flags & QSES_FLAG_KEEP_DEGENERATE) != 0;
     HostDownload &dl = ctx->dl;
     if (dl.want) {  // [vertices | triangles (pre-filter count) | atom_sorted | atom_input]
@@ -420,71 +727,68 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         dl.ab = 4ull * nv;
         dl.block = pinned_take(dl.vb + dl.tb + 2 * dl.ab + 64, &dl.bytes);
         if (!dl.block) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned host mesh");
+        dl.d2h = dl.vb + dl.tb + 2 * dl.ab;
     }
-    if (fork) {
-        QCHK(cudaEventRecord(ctx->ev_fork, s));
-        QCHK(cudaStreamWaitEvent(sd, ctx->ev_fork, 0));
-    }
-
-    // ---- closest atom per welded vertex (before smoothing, as in the reference)
-    if (nv > 0) {
-        launch_closest(g, vq, nv, atoms, cells, sidx, asorted, ainput, sd);
-        ctx->launches++;
-    }
-    ctx->mark("closest_atom");
-
-    // ---- drop degenerate triangles (API_computeSES filter)
-    if (!keep_all && T > 0) {
-        launch_tri_flags(tri, T, tflags, sd);
-        ctx->launches++;
-        QCHK(scan_u2(tflags, tflags, T, d_tot, tmp2, d_err, sd, &ctx->launches));
-        launch_tri_compact(tri, T, tflags, tri_kept, sd);
-        ctx->launches++;
-        QCHK(cudaMemcpyAsync(ctx->h_small, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, sd));
-    }
-    ctx->mark("filter");
-    const unsigned *tri_out = keep_all ? tri : tri_kept;
+    FinishSeg c;
+    memset(&c, 0, sizeof(c));
+    c.atoms = a.atoms;
+    c.cells = a.cells;
+    c.sidx = sidx;
+    c.asorted = asorted;
+    c.ainput = ainput;
+    c.vq = vq;
+    c.tri = tri;
+    c.tri_kept = tri_kept;
+    c.tflags = tflags;
+    c.tmp2 = tmp2;
+    c.tot = a.tot;
+    c.err = d_err;
+    c.h_out = ctx->h_small;
     if (dl.want) {
-        char *hb = (char *)dl.block;
-        if (dl.tb) QCHK(cudaMemcpyAsync(hb + dl.vb, tri_out, dl.tb, cudaMemcpyDeviceToHost, sd));
-        if (dl.ab) QCHK(cudaMemcpyAsync(hb + dl.vb + dl.tb, asorted, dl.ab, cudaMemcpyDeviceToHost, sd));
-        if (dl.ab) QCHK(cudaMemcpyAsync(hb + dl.vb + dl.tb + dl.ab, ainput, dl.ab, cudaMemcpyDeviceToHost, sd));
-        dl.d2h = dl.tb + 2 * dl.ab;
+        c.h_dl = (char *)dl.block;
+        c.dl_vb = dl.vb;
+        c.dl_tb = dl.tb;
+        c.dl_ab = dl.ab;
     }
-    if (fork) QCHK(cudaEventRecord(ctx->ev_join, sd));
-
-    // ---- Gauss-Seidel smoothing on the device
-    if (p.smooth_passes > 0 && nv > 0 && T > 0) {
-        uint2 *deg = flags;  // reuse: nv + 1 <= NE + 1 entries
-        QCHK(cudaMemsetAsync(deg, 0, 8ull * (nv + 1), s));
-        launch_degree(tri, n3, nv, deg, s);
-        ctx->launches++;
-        QCHK(scan_u2(deg, deg, nv + 1, nullptr, tmpb, d_err, s, &ctx->launches));
-        launch_copy_keys(tri, n3, okey, s);
-        ctx->launches++;
-        QCHK(radix_sort<unsigned>(okey, okey2, oval, oval2, (unsigned)n3, bits_for(nv - 1), true, tmpb, d_err, s,
-                                  &ctx->launches, &alt));
-        unsigned *socc = alt ? oval2 : oval;
-        launch_csr_fill(tri, socc, n3, nbr, s);
-        ctx->launches++;
-        ctx->mark("smooth_csr");
-        const GsShape sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(nv, false);
-        ctx->gs_used = sh;
-        unsigned long long *stats = (unsigned long long *)((char *)ctx->small + 256);
-        // the closest-atom pass on the side stream reads the welded positions in vq
-        int rc2 = run_smoothing(ctx, sh, p.smooth_passes, vq, pos4, nv, deg, nbr, (unsigned short *)cnt, lower, inbox,
-                                inbox_tail, d_err, stats, true, fork ? ctx->ev_join : nullptr);
-        if (rc2) return rc2;
+    c.deg = flags;  // reuse: nv + 1 <= NE + 1 entries
+    c.okey = okey;
+    c.okey2 = okey2;
+    c.oval = oval;
+    c.oval2 = oval2;
+    c.nbr = nbr;
+    c.tmpb = tmpb;
+    c.pos4 = pos4;
+    c.cnt = (unsigned short *)cnt;
+    c.lower = lower;
+    c.stats = (unsigned long long *)((char *)ctx->small + 256);
+    c.n3 = n3;
+    c.nv = nv;
+    c.nt = T;
+    c.passes = p.smooth_passes;
+    c.keep_all = keep_all;
+    c.fork = !ctx->profiling && ctx->side != nullptr;
+    const bool smoothing = p.smooth_passes > 0 && nv > 0 && T > 0;
+    if (smoothing) {
+        c.sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(nv, false);
+        ctx->gs_used = c.sh;
+        GsPlan plan;
+        rc = gs_plan(ctx->device, c.sh, nv, nullptr, nullptr, 1, plan);
+        if (rc != QSES_OK) return ctx->fail(rc, "smoothing slab plan");
+        GsBuffers gb;
+        QCHK_RC(gs_buffers(ctx, plan, nv, gb));
+        c.gl = plan.L;
+        c.home = gb.home;
+        c.table = gb.table;
+        c.h_table = ctx->h_gs;
+        c.inbox = gb.inbox;
+        c.inbox_tail = gb.inbox_tail;
+        ctx->diag[0] = plan.max_slabs;
+        ctx->diag[1] = plan.max_len;
     }
-    ctx->mark("smooth");
-    if (dl.want && dl.vb) {
-        QCHK(cudaMemcpyAsync(dl.block, vq, dl.vb, cudaMemcpyDeviceToHost, s));
-        dl.d2h += dl.vb;
-    }
-    if (fork) QCHK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
-
-    QCHK(cudaMemcpyAsync(ctx->h_small + 8, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    QCHK(cudaMemcpyAsync(ctx->h_small + 2048, (char *)ctx->small + 256, 64, cudaMemcpyDeviceToHost, s));
+    c.g = g;
+    SegOut oc;
+    // an L2 persistence window is a stream attribute, set when the launch is enqueued
+    QCHK_RC(run_segment(ctx, kSegFinish, c, oc, enqueue_finish, !(smoothing && (c.sh.flags & kGsPersistL2))));
     QCHK(cudaStreamSynchronize(s));
     ctx->mark("download");
     memcpy(ctx->diag + 2, ctx->h_small + 2048, 7 * sizeof(unsigned long long));
@@ -504,7 +808,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     m.triangles = keep_all ? tri : tri_kept;
     m.atom_sorted = asorted;
     m.atom_input = ainput;
-    m.codes = codes;
+    m.codes = a.codes;
     m.sorted_to_input = sidx;
     m.sorted_keys = skey;
     m.n_atoms = n;

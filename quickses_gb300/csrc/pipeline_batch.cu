@@ -25,6 +25,7 @@
 #include "kernels.h"
 #include "prims.h"
 #include "qses_context.h"
+#include "segment.h"
 
 namespace qses {
 
@@ -32,6 +33,12 @@ namespace qses {
     do {                                                                                \
         cudaError_t e_ = (expr);                                                        \
         if (e_ != cudaSuccess) return ctx->fail(QSES_ERR_CUDA, #expr, e_);              \
+    } while (0)
+
+#define QCHK_RC(expr)                                                                   \
+    do {                                                                                \
+        const int rc_ = (expr);                                                         \
+        if (rc_ != QSES_OK) return rc_;                                                 \
     } while (0)
 
 static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -49,6 +56,216 @@ static int stage_reserve(qses_context *ctx, size_t bytes) {
         return QSES_ERR_OUT_OF_MEMORY;
     }
     ctx->h_stage_cap = want;
+    return QSES_OK;
+}
+
+// ---- segment 1: descriptors and atoms up, atoms sorted into cells, field, row counts
+struct BatchFieldSeg {
+    const char *h_desc;  // pinned staging; the copy nodes read it when the segment runs
+    char *d_desc;
+    const float *h_x;
+    float *d_x;
+    unsigned long long desc_bytes, atom_bytes;
+    unsigned *key, *key2, *idx, *idx2;
+    float4 *atoms;
+    uint2 *cells;
+    unsigned *in_mask, *out_mask, *sign_mask;
+    unsigned char *codes;
+    uint2 *rows, *tot;
+    unsigned *counters;
+    void *tmp;
+    int *err;
+    unsigned *tri_off, *edge_off;
+    unsigned char *h_out;  // pinned: [0, 8) totals, [8, 12) error word
+    unsigned long long cell_tot, n_rows;
+    unsigned n, tiles, units;
+    int cell_bits;
+    QBatch b;
+};
+
+static int enqueue_batch_field(qses_context *ctx, const BatchFieldSeg &a, SegOut &o) {
+    cudaStream_t s = ctx->stream;
+    QCHK(cudaMemcpyAsync(a.d_desc, a.h_desc, a.desc_bytes, cudaMemcpyHostToDevice, s));
+    QCHK(cudaMemcpyAsync(a.d_x, a.h_x, a.atom_bytes, cudaMemcpyHostToDevice, s));
+    QCHK(cudaMemsetAsync(a.err, 0, sizeof(int), s));
+    QCHK(cudaMemsetAsync(a.counters, 0, 64, s));
+    // atoms
+    launch_atom_hash_batch(a.b, a.d_x, a.n, a.key, s);
+    ctx->launches++;
+    QCHK(radix_sort<unsigned>(a.key, a.key2, a.idx, a.idx2, a.n, a.cell_bits, true, a.tmp, a.err, s, &ctx->launches,
+                              &o.alt));
+    const unsigned *skey = o.alt ? a.key2 : a.key, *sidx = o.alt ? a.idx2 : a.idx;
+    QCHK(cudaMemsetAsync(a.cells, 0, 8 * a.cell_tot, s));
+    launch_atom_gather(a.d_x, a.d_x + 3ull * a.n, skey, sidx, a.n, a.atoms, a.cells, s);
+    ctx->launches++;
+    ctx->mark("atoms");
+    // field: persistent CTAs over (molecule, tile) items
+    launch_sas_batch(a.b, a.tiles, a.atoms, a.cells, a.in_mask, a.out_mask, a.counters, s);
+    ctx->launches++;
+    ctx->mark("sas");
+    launch_edt_batch(a.b, a.tiles, a.in_mask, a.out_mask, a.codes, a.sign_mask, a.counters + 1, s);
+    ctx->launches++;
+    ctx->mark("refine");
+    // marching-cubes counts, one scan over all rows, per-molecule offsets
+    launch_mc_count_batch(a.b, a.units, a.sign_mask, a.rows, s);
+    ctx->launches++;
+    QCHK(scan_u2(a.rows, a.rows, (unsigned)a.n_rows, a.tot, a.tmp, a.err, s, &ctx->launches));
+    launch_gather_offsets(a.rows, a.b.row_off, a.b.n_mol, (unsigned)a.n_rows, a.tot, a.tri_off, a.edge_off, s);
+    ctx->launches++;
+    QCHK(cudaMemcpyAsync(a.h_out, a.tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    QCHK(cudaMemcpyAsync(a.h_out + 8, a.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return QSES_OK;
+}
+
+// ---- segment 2: triangles and molecule-tagged weld keys, one weld for all molecules
+struct BatchMeshSeg {
+    const unsigned *sign_mask;
+    const unsigned char *codes;
+    const uint2 *rows;
+    unsigned *tri;
+    unsigned long long *vk, *vk2;
+    unsigned *vv, *vv2;
+    uint2 *flags, *tot;
+    unsigned *vmap;
+    float *vq;
+    unsigned *vmol;
+    void *tmp;
+    int *err;
+    unsigned *edge_off, *vtx_off;
+    unsigned char *h_out;  // pinned: [0, 8) vertex total
+    void *h_vtx;           // pinned: per-molecule first vertex
+    unsigned long long n3;
+    unsigned units, ne;
+    int tot_bits, pad_;
+    QBatch b;
+};
+
+static int enqueue_batch_mesh(qses_context *ctx, const BatchMeshSeg &m, SegOut &o) {
+    cudaStream_t s = ctx->stream;
+    const unsigned nm = m.b.n_mol;
+    launch_mc_emit_batch(m.b, m.units, m.sign_mask, m.codes, m.rows, m.tri, m.vk, s);
+    ctx->launches++;
+    ctx->mark("mc_emit");
+    if (m.ne > 0) {
+        QCHK(radix_sort<unsigned long long>(m.vk, m.vk2, m.vv, m.vv2, m.ne, m.tot_bits, true, m.tmp, m.err, s,
+                                            &ctx->launches, &o.alt));
+        const unsigned long long *sk = o.alt ? m.vk2 : m.vk;
+        const unsigned *sv = o.alt ? m.vv2 : m.vv;
+        launch_weld_flags(sk, m.ne, m.flags, s);
+        ctx->launches++;
+        QCHK(scan_u2(m.flags, m.flags, m.ne, m.tot, m.tmp, m.err, s, &ctx->launches));
+        launch_weld_scatter_batch(m.b, sk, sv, m.flags, m.ne, m.vmap, m.vq, m.vmol, s);
+        ctx->launches++;
+        // molecule k's edges occupy sorted positions [edge_off[k], edge_off[k+1]) (its keys
+        // sort between the other molecules'), so its first vertex is the rank there
+        launch_gather_offsets(m.flags, m.edge_off, nm, m.ne, m.tot, m.vtx_off, nullptr, s);
+        ctx->launches++;
+        launch_remap(m.tri, m.n3, m.vmap, s);
+        ctx->launches++;
+    } else {
+        QCHK(cudaMemsetAsync(m.vtx_off, 0, 4ull * (nm + 1), s));
+    }
+    QCHK(cudaMemcpyAsync(m.h_out, m.tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    QCHK(cudaMemcpyAsync(m.h_vtx, m.vtx_off, 4ull * (nm + 1), cudaMemcpyDeviceToHost, s));
+    return QSES_OK;
+}
+
+// ---- segment 3: closest atom, per-molecule filter and host downloads on the side stream;
+// neighbour lists and one Gauss-Seidel dataflow over all molecules on the main stream
+struct BatchFinishSeg {
+    const float4 *atoms;
+    const uint2 *cells;
+    const unsigned *sidx, *vmol;
+    int *asorted, *ainput;
+    float *vq;
+    unsigned *tri, *tri_kept;
+    uint2 *tflags;
+    void *tmp2;
+    uint2 *tot;
+    int *err;
+    unsigned *tri_off, *kept_off;
+    unsigned char *h_out;  // pinned: [0, 8) kept triangles, [8, 12) error word
+    void *h_kept;          // pinned: per-molecule first kept triangle
+    char *h_dl;            // pinned host mesh block, or null
+    unsigned long long dl_vb, dl_tb, dl_ab;
+    uint2 *deg;
+    unsigned *okey, *okey2, *oval, *oval2, *nbr;
+    void *tmpb;
+    float4 *pos4;
+    unsigned short *cnt;
+    int *lower;
+    uint2 *home;
+    unsigned *table;
+    const unsigned *h_table;  // pinned slab tables; the copy node reads them when the segment runs
+    unsigned *inbox, *inbox_tail;
+    unsigned long long n3;
+    unsigned nv, nt;
+    int passes, fork;
+    GsShape sh;
+    GsLaunch gl;
+    QBatch b;
+};
+
+static int enqueue_batch_finish(qses_context *ctx, const BatchFinishSeg &c, SegOut &o) {
+    cudaStream_t s = ctx->stream, sd = c.fork ? ctx->side : s;
+    const unsigned nm = c.b.n_mol;
+    if (c.fork) {
+        QCHK(cudaEventRecord(ctx->ev_fork, s));
+        QCHK(cudaStreamWaitEvent(sd, ctx->ev_fork, 0));
+    }
+    if (c.nv > 0) {
+        launch_closest_batch(c.b, c.vq, c.vmol, c.nv, c.atoms, c.cells, c.sidx, c.asorted, c.ainput, sd);
+        ctx->launches++;
+    }
+    ctx->mark("closest_atom");
+    // per-molecule filter and molecule-local corner ids
+    if (c.nt > 0) {
+        launch_tri_flags_batch(c.b, c.tri, c.nt, c.tflags, sd);
+        ctx->launches++;
+        QCHK(scan_u2(c.tflags, c.tflags, c.nt, c.tot, c.tmp2, c.err, sd, &ctx->launches));
+        launch_tri_compact_batch(c.b, c.tri, c.nt, c.tflags, c.tri_kept, sd);
+        ctx->launches++;
+        launch_gather_offsets(c.tflags, c.tri_off, nm, c.nt, c.tot, c.kept_off, nullptr, sd);
+        ctx->launches++;
+    } else {
+        QCHK(cudaMemsetAsync(c.kept_off, 0, 4ull * (nm + 1), sd));
+        QCHK(cudaMemsetAsync(c.tot, 0, sizeof(uint2), sd));
+    }
+    QCHK(cudaMemcpyAsync(c.h_out, c.tot, sizeof(uint2), cudaMemcpyDeviceToHost, sd));
+    QCHK(cudaMemcpyAsync(c.h_kept, c.kept_off, 4ull * (nm + 1), cudaMemcpyDeviceToHost, sd));
+    ctx->mark("filter");
+    if (c.h_dl) {
+        if (c.dl_tb) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb, c.tri_kept, c.dl_tb, cudaMemcpyDeviceToHost, sd));
+        if (c.dl_ab) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb, c.asorted, c.dl_ab, cudaMemcpyDeviceToHost, sd));
+        if (c.dl_ab)
+            QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb + c.dl_ab, c.ainput, c.dl_ab, cudaMemcpyDeviceToHost, sd));
+    }
+    if (c.fork) QCHK(cudaEventRecord(ctx->ev_join, sd));
+
+    // Gauss-Seidel over all molecules
+    if (c.passes > 0 && c.nv > 0 && c.nt > 0) {
+        QCHK(cudaMemsetAsync(c.deg, 0, 8ull * (c.nv + 1), s));
+        launch_degree(c.tri, c.n3, c.nv, c.deg, s);
+        ctx->launches++;
+        QCHK(scan_u2(c.deg, c.deg, c.nv + 1, nullptr, c.tmpb, c.err, s, &ctx->launches));
+        launch_copy_keys(c.tri, c.n3, c.okey, s);
+        ctx->launches++;
+        QCHK(radix_sort<unsigned>(c.okey, c.okey2, c.oval, c.oval2, (unsigned)c.n3, bits_for(c.nv - 1), true, c.tmpb,
+                                  c.err, s, &ctx->launches, &o.alt));
+        const unsigned *socc = o.alt ? c.oval2 : c.oval;
+        launch_csr_fill(c.tri, socc, c.n3, c.nbr, s);
+        ctx->launches++;
+        ctx->mark("smooth_csr");
+        // the closest-atom pass on the side stream reads the welded positions in vq
+        const int rc = run_smoothing(ctx, c.sh, c.gl, c.passes, c.vq, c.pos4, c.nv, c.deg, c.nbr, c.cnt, c.lower,
+                                     c.home, c.table, c.h_table, c.inbox, c.inbox_tail, c.err, nullptr,
+                                     c.fork ? ctx->ev_join : nullptr);
+        if (rc) return rc;
+    }
+    ctx->mark("smooth");
+    if (c.h_dl && c.dl_vb) QCHK(cudaMemcpyAsync(c.h_dl, c.vq, c.dl_vb, cudaMemcpyDeviceToHost, s));
+    if (c.fork) QCHK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    QCHK(cudaMemcpyAsync(c.h_out + 8, c.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     return QSES_OK;
 }
 
@@ -142,17 +359,20 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
                          3 * a256(4 * mask_tot) + a256(code_tot) + a256(8 * rows) + 2 * a256(64) + a256(tmpA) + 8192;
     if (ctx->field.reserve(needA) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "batch field workspace");
     Arena &A = ctx->field;
-    char *d_desc = (char *)A.take(desc_bytes);
-    float *d_x = (float *)A.take(16ull * N);
-    QCHK(cudaMemcpyAsync(d_desc, hs, desc_bytes, cudaMemcpyHostToDevice, s));
-    QCHK(cudaMemcpyAsync(d_x, hx, atom_bytes, cudaMemcpyHostToDevice, s));
-    const float *d_r = d_x + 3ull * N;
-    QBatch b;
+    BatchFieldSeg a;
+    memset(&a, 0, sizeof(a));
+    a.h_desc = hs;
+    a.d_desc = (char *)A.take(desc_bytes);
+    a.h_x = hx;
+    a.d_x = (float *)A.take(16ull * N);
+    a.desc_bytes = desc_bytes;
+    a.atom_bytes = atom_bytes;
+    QBatch &b = a.b;
     unsigned *d_edge_off, *d_kept_off;
     {
         size_t q = 0;
         auto at = [&](size_t bytes) {
-            char *p = d_desc + q;
+            char *p = a.d_desc + q;
             q += a256(bytes);
             return p;
         };
@@ -171,51 +391,36 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         b.key_bits = key_bits;
     }
     unsigned *d_tri_off = (unsigned *)b.tri_off, *d_vtx_off = (unsigned *)b.vtx_off;
-
-    unsigned *key = (unsigned *)A.take(4ull * N), *key2 = (unsigned *)A.take(4ull * N);
-    unsigned *idx = (unsigned *)A.take(4ull * N), *idx2 = (unsigned *)A.take(4ull * N);
-    float4 *atoms = (float4 *)A.take(16ull * N);
-    uint2 *cells = (uint2 *)A.take(8 * cell_tot);
-    unsigned *inMask = (unsigned *)A.take(4 * mask_tot), *outMask = (unsigned *)A.take(4 * mask_tot);
-    unsigned *signMask = (unsigned *)A.take(4 * mask_tot);
-    unsigned char *codes = (unsigned char *)A.take(code_tot);
-    uint2 *rowsb = (uint2 *)A.take(8 * rows);
-    uint2 *d_tot = (uint2 *)A.take(64);
-    unsigned *counters = (unsigned *)A.take(64);
-    void *tmp = A.take(tmpA);
-    if (!tmp) return ctx->fail(QSES_ERR_INTERNAL, "batch field workspace layout");
+    a.key = (unsigned *)A.take(4ull * N);
+    a.key2 = (unsigned *)A.take(4ull * N);
+    a.idx = (unsigned *)A.take(4ull * N);
+    a.idx2 = (unsigned *)A.take(4ull * N);
+    a.atoms = (float4 *)A.take(16ull * N);
+    a.cells = (uint2 *)A.take(8 * cell_tot);
+    a.in_mask = (unsigned *)A.take(4 * mask_tot);
+    a.out_mask = (unsigned *)A.take(4 * mask_tot);
+    a.sign_mask = (unsigned *)A.take(4 * mask_tot);
+    a.codes = (unsigned char *)A.take(code_tot);
+    a.rows = (uint2 *)A.take(8 * rows);
+    a.tot = (uint2 *)A.take(64);
+    a.counters = (unsigned *)A.take(64);
+    a.tmp = A.take(tmpA);
+    if (!a.tmp) return ctx->fail(QSES_ERR_INTERNAL, "batch field workspace layout");
     int *d_err = (int *)((char *)ctx->small + 64);
-    QCHK(cudaMemsetAsync(d_err, 0, sizeof(int), s));
-    QCHK(cudaMemsetAsync(counters, 0, 64, s));
-
-    // ---- atoms
-    launch_atom_hash_batch(b, d_x, N, key, s);
-    ctx->launches++;
-    int alt = 0;
-    QCHK(radix_sort<unsigned>(key, key2, idx, idx2, N, cell_bits, true, tmp, d_err, s, &ctx->launches, &alt));
-    unsigned *skey = alt ? key2 : key, *sidx = alt ? idx2 : idx;
-    QCHK(cudaMemsetAsync(cells, 0, 8 * cell_tot, s));
-    launch_atom_gather(d_x, d_r, skey, sidx, N, atoms, cells, s);
-    ctx->launches++;
-    ctx->mark("atoms");
-
-    // ---- field: persistent CTAs over (molecule, tile) items
-    launch_sas_batch(b, (unsigned)tiles, atoms, cells, inMask, outMask, counters, s);
-    ctx->launches++;
-    ctx->mark("sas");
-    launch_edt_batch(b, (unsigned)tiles, inMask, outMask, codes, signMask, counters + 1, s);
-    ctx->launches++;
-    ctx->mark("refine");
-
-    // ---- marching-cubes counts, one scan over all rows, per-molecule offsets
-    launch_mc_count_batch(b, (unsigned)units, signMask, rowsb, s);
-    ctx->launches++;
-    QCHK(scan_u2(rowsb, rowsb, (unsigned)rows, d_tot, tmp, d_err, s, &ctx->launches));
-    launch_gather_offsets(rowsb, b.row_off, nm, (unsigned)rows, d_tot, d_tri_off, d_edge_off, s);
-    ctx->launches++;
+    a.err = d_err;
+    a.tri_off = d_tri_off;
+    a.edge_off = d_edge_off;
+    a.h_out = ctx->h_small;
+    a.cell_tot = cell_tot;
+    a.n_rows = rows;
+    a.n = N;
+    a.tiles = (unsigned)tiles;
+    a.units = (unsigned)units;
+    a.cell_bits = cell_bits;
+    SegOut oa;
+    QCHK_RC(run_segment(ctx, kSegBatchField, a, oa, enqueue_batch_field));
+    const unsigned *sidx = oa.alt ? a.idx2 : a.idx;
     unsigned *hsm = (unsigned *)ctx->h_small;  // 4 KB pinned: totals and the error word
-    QCHK(cudaMemcpyAsync(hsm, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
-    QCHK(cudaMemcpyAsync(hsm + 2, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     QCHK(cudaStreamSynchronize(s));
     ctx->mark("mc_count");
     if (hsm[2]) return ctx->fail((int)hsm[2], "device wait in the batch field stage");
@@ -231,8 +436,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     const size_t nflag = std::max<size_t>((size_t)NE + 1, (size_t)T) + 1;
     const size_t needB = 2 * a256(4 * n3 + 4) + 2 * a256(8ull * NE + 8) + 2 * a256(4ull * NE + 4) +
                          a256(8ull * nflag) + a256(4ull * NE + 4) + a256(12ull * NE + 12) + 3 * a256(4ull * NE + 4) +
-                         4 * a256(4 * n3 + 4) + a256(8 * n3 + 8) + 3 * a256(4ull * NE + 4) + a256(4ull * NE + 65536) +
-                         a256(4096) + a256(16ull * NE + 16) + a256(tmpB) + a256(8ull * T + 16) +
+                         4 * a256(4 * n3 + 4) + a256(8 * n3 + 8) + 3 * a256(4ull * NE + 4) + a256(16ull * NE + 16) + a256(tmpB) + a256(8ull * T + 16) +
                          a256(scan_u2_tmp_bytes(T + 1)) + 8192;
     if (ctx->mesh_ws.reserve(needB) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "batch mesh workspace");
     Arena &B = ctx->mesh_ws;
@@ -249,8 +453,6 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     unsigned *oval = (unsigned *)B.take(4 * n3 + 4), *oval2 = (unsigned *)B.take(4 * n3 + 4);
     unsigned *nbr = (unsigned *)B.take(8 * n3 + 8);
     int *lower = (int *)B.take(4ull * NE + 4), *cnt = (int *)B.take(4ull * NE + 4);
-    unsigned *inbox = (unsigned *)B.take(4ull * NE + 65536);
-    unsigned *inbox_tail = (unsigned *)B.take(4096);
     float4 *pos4 = (float4 *)B.take(16ull * NE + 16);
     void *tmpb = B.take(tmpB);
     uint2 *tflags = (uint2 *)B.take(8ull * T + 16);  // degenerate filter (side stream)
@@ -258,42 +460,43 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     if (!tmpb || !tflags || !tmp2) return ctx->fail(QSES_ERR_INTERNAL, "batch mesh workspace layout");
 
     // ---- triangles + molecule-tagged weld keys, then one weld for all molecules
-    launch_mc_emit_batch(b, (unsigned)units, signMask, codes, rowsb, tri, vk, s);
-    ctx->launches++;
-    ctx->mark("mc_emit");
-    unsigned nv = 0;
-    if (NE > 0) {
-        QCHK(radix_sort<unsigned long long>(vk, vk2, vv, vv2, NE, tot_bits, true, tmpb, d_err, s, &ctx->launches,
-                                            &alt));
-        unsigned long long *sk = alt ? vk2 : vk;
-        unsigned *sv = alt ? vv2 : vv;
-        launch_weld_flags(sk, NE, flags, s);
-        ctx->launches++;
-        QCHK(scan_u2(flags, flags, NE, d_tot, tmpb, d_err, s, &ctx->launches));
-        launch_weld_scatter_batch(b, sk, sv, flags, NE, vmap, vq, vmol, s);
-        ctx->launches++;
-        // molecule m's edges occupy sorted positions [edge_off[m], edge_off[m+1]) (its keys
-        // sort between the other molecules'), so its first vertex is the rank there
-        launch_gather_offsets(flags, d_edge_off, nm, NE, d_tot, d_vtx_off, nullptr, s);
-        ctx->launches++;
-        launch_remap(tri, n3, vmap, s);
-        ctx->launches++;
-    } else {
-        QCHK(cudaMemsetAsync(d_vtx_off, 0, 4ull * (nm + 1), s));
-    }
-    std::vector<unsigned> vtx_off(nm + 1);
-    QCHK(cudaMemcpyAsync(hsm, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, s));
-    QCHK(cudaMemcpyAsync(ctx->h_stage, d_vtx_off, 4ull * (nm + 1), cudaMemcpyDeviceToHost, s));
+    BatchMeshSeg mb;
+    memset(&mb, 0, sizeof(mb));
+    mb.sign_mask = a.sign_mask;
+    mb.codes = a.codes;
+    mb.rows = a.rows;
+    mb.tri = tri;
+    mb.vk = vk;
+    mb.vk2 = vk2;
+    mb.vv = vv;
+    mb.vv2 = vv2;
+    mb.flags = flags;
+    mb.tot = a.tot;
+    mb.vmap = vmap;
+    mb.vq = vq;
+    mb.vmol = vmol;
+    mb.tmp = tmpb;
+    mb.err = d_err;
+    mb.edge_off = d_edge_off;
+    mb.vtx_off = d_vtx_off;
+    mb.h_out = ctx->h_small;
+    mb.h_vtx = ctx->h_stage;
+    mb.n3 = n3;
+    mb.units = (unsigned)units;
+    mb.ne = NE;
+    mb.tot_bits = tot_bits;
+    mb.b = b;
+    SegOut ob;
+    QCHK_RC(run_segment(ctx, kSegBatchMesh, mb, ob, enqueue_batch_mesh));
     QCHK(cudaStreamSynchronize(s));
+    std::vector<unsigned> vtx_off(nm + 1);
     memcpy(vtx_off.data(), ctx->h_stage, 4ull * (nm + 1));
-    nv = NE > 0 ? hsm[0] : 0;
+    const unsigned nv = NE > 0 ? hsm[0] : 0;
     ctx->mark("weld");
 
     // Closest atom, filter and (for host results) the triangle and atom-id downloads run on
     // the side stream beside the neighbour-list build and the smoothing; profiled calls keep
     // one stream so the stage times stay separable.
-    const bool fork = !ctx->profiling && ctx->side != nullptr;
-    cudaStream_t sd = fork ? ctx->side : s;
     HostDownload &dl = ctx->dl;
     if (dl.want) {  // [vertices | triangles (pre-filter count) | atom_sorted | atom_input]
         dl.vb = 12ull * nv;
@@ -301,77 +504,79 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         dl.ab = 4ull * nv;
         dl.block = pinned_take(dl.vb + dl.tb + 2 * dl.ab + 256, &dl.bytes);
         if (!dl.block) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned batch meshes");
+        dl.d2h = dl.vb + dl.tb + 2 * dl.ab;
     }
-    if (fork) {
-        QCHK(cudaEventRecord(ctx->ev_fork, s));
-        QCHK(cudaStreamWaitEvent(sd, ctx->ev_fork, 0));
-    }
-    if (nv > 0) {
-        launch_closest_batch(b, vq, vmol, nv, atoms, cells, sidx, asorted, ainput, sd);
-        ctx->launches++;
-    }
-    ctx->mark("closest_atom");
-
-    // ---- per-molecule filter and molecule-local corner ids
-    if (T > 0) {
-        launch_tri_flags_batch(b, tri, T, tflags, sd);
-        ctx->launches++;
-        QCHK(scan_u2(tflags, tflags, T, d_tot, tmp2, d_err, sd, &ctx->launches));
-        launch_tri_compact_batch(b, tri, T, tflags, tri_kept, sd);
-        ctx->launches++;
-        launch_gather_offsets(tflags, d_tri_off, nm, T, d_tot, d_kept_off, nullptr, sd);
-        ctx->launches++;
-    } else {
-        QCHK(cudaMemsetAsync(d_kept_off, 0, 4ull * (nm + 1), sd));
-        QCHK(cudaMemsetAsync(d_tot, 0, sizeof(uint2), sd));
-    }
-    QCHK(cudaMemcpyAsync(hsm, d_tot, sizeof(uint2), cudaMemcpyDeviceToHost, sd));
-    QCHK(cudaMemcpyAsync(ctx->h_stage, d_kept_off, 4ull * (nm + 1), cudaMemcpyDeviceToHost, sd));
-    ctx->mark("filter");
+    BatchFinishSeg c;
+    memset(&c, 0, sizeof(c));
+    c.atoms = a.atoms;
+    c.cells = a.cells;
+    c.sidx = sidx;
+    c.vmol = vmol;
+    c.asorted = asorted;
+    c.ainput = ainput;
+    c.vq = vq;
+    c.tri = tri;
+    c.tri_kept = tri_kept;
+    c.tflags = tflags;
+    c.tmp2 = tmp2;
+    c.tot = a.tot;
+    c.err = d_err;
+    c.tri_off = d_tri_off;
+    c.kept_off = d_kept_off;
+    c.h_out = ctx->h_small;
+    c.h_kept = ctx->h_stage;
     if (dl.want) {
-        char *hb = (char *)dl.block;
-        if (dl.tb) QCHK(cudaMemcpyAsync(hb + dl.vb, tri_kept, dl.tb, cudaMemcpyDeviceToHost, sd));
-        if (dl.ab) QCHK(cudaMemcpyAsync(hb + dl.vb + dl.tb, asorted, dl.ab, cudaMemcpyDeviceToHost, sd));
-        if (dl.ab) QCHK(cudaMemcpyAsync(hb + dl.vb + dl.tb + dl.ab, ainput, dl.ab, cudaMemcpyDeviceToHost, sd));
-        dl.d2h = dl.tb + 2 * dl.ab;
+        c.h_dl = (char *)dl.block;
+        c.dl_vb = dl.vb;
+        c.dl_tb = dl.tb;
+        c.dl_ab = dl.ab;
     }
-    if (fork) QCHK(cudaEventRecord(ctx->ev_join, sd));
-
-    // ---- Gauss-Seidel over all molecules
-    if (passes > 0 && nv > 0 && T > 0) {
-        uint2 *deg = flags;
-        QCHK(cudaMemsetAsync(deg, 0, 8ull * (nv + 1), s));
-        launch_degree(tri, n3, nv, deg, s);
-        ctx->launches++;
-        QCHK(scan_u2(deg, deg, nv + 1, nullptr, tmpb, d_err, s, &ctx->launches));
-        launch_copy_keys(tri, n3, okey, s);
-        ctx->launches++;
-        QCHK(radix_sort<unsigned>(okey, okey2, oval, oval2, (unsigned)n3, bits_for(nv - 1), true, tmpb, d_err, s,
-                                  &ctx->launches, &alt));
-        unsigned *socc = alt ? oval2 : oval;
-        launch_csr_fill(tri, socc, n3, nbr, s);
-        ctx->launches++;
-        ctx->mark("smooth_csr");
-        const GsShape sh = ctx->gs_force.threads ? ctx->gs_force
-                                                  : gs_shape(std::min<unsigned>(nv, 152u * kGsSlabMaxVerts), true);
-        ctx->gs_used = sh;
-        // the closest-atom pass on the side stream reads the welded positions in vq
-        int rc2 = run_smoothing(ctx, sh, passes, vq, pos4, nv, deg, nbr, (unsigned short *)cnt, lower, inbox,
-                                inbox_tail, d_err, nullptr, true, fork ? ctx->ev_join : nullptr);
-        if (rc2) return rc2;
+    c.deg = flags;
+    c.okey = okey;
+    c.okey2 = okey2;
+    c.oval = oval;
+    c.oval2 = oval2;
+    c.nbr = nbr;
+    c.tmpb = tmpb;
+    c.pos4 = pos4;
+    c.cnt = (unsigned short *)cnt;
+    c.lower = lower;
+    c.n3 = n3;
+    c.nv = nv;
+    c.nt = T;
+    c.passes = passes;
+    c.fork = !ctx->profiling && ctx->side != nullptr;
+    const bool smoothing = passes > 0 && nv > 0 && T > 0;
+    if (smoothing) {
+        c.sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(std::min<unsigned>(nv, 152u * kGsSlabMaxVerts), true);
+        ctx->gs_used = c.sh;
+        // molecules are never split between slabs unless larger than one; their grid sizes
+        // estimate the dependency depths that order the slabs
+        std::vector<int> depth(nm);
+        for (unsigned m = 0; m < nm; m++) depth[m] = items[m].g.G;
+        GsPlan plan;
+        const int rp = gs_plan(ctx->device, c.sh, nv, vtx_off.data(), depth.data(), nm, plan);
+        if (rp != QSES_OK) return ctx->fail(rp, "smoothing slab plan");
+        GsBuffers gb;
+        QCHK_RC(gs_buffers(ctx, plan, nv, gb));
+        c.gl = plan.L;
+        c.home = gb.home;
+        c.table = gb.table;
+        c.h_table = ctx->h_gs;
+        c.inbox = gb.inbox;
+        c.inbox_tail = gb.inbox_tail;
+        ctx->diag[0] = std::max<unsigned long long>(ctx->diag[0], plan.max_slabs);
+        ctx->diag[1] = std::max<unsigned long long>(ctx->diag[1], plan.max_len);
     }
-    ctx->mark("smooth");
-    if (dl.want && dl.vb) {
-        QCHK(cudaMemcpyAsync(dl.block, vq, dl.vb, cudaMemcpyDeviceToHost, s));
-        dl.d2h += dl.vb;
-    }
-    if (fork) QCHK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
-    std::vector<unsigned> kept_off(nm + 1);
-    QCHK(cudaMemcpyAsync(hsm + 2, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    c.b = b;
+    SegOut oc;
+    // an L2 persistence window is a stream attribute, set when the launch is enqueued
+    QCHK_RC(run_segment(ctx, kSegBatchFinish, c, oc, enqueue_batch_finish, !(smoothing && (c.sh.flags & kGsPersistL2))));
     QCHK(cudaStreamSynchronize(s));
     ctx->mark("download");
     if (hsm[2]) return ctx->fail((int)hsm[2], "device wait in the batch mesh stage");
     const unsigned nkept = hsm[0];
+    std::vector<unsigned> kept_off(nm + 1);
     memcpy(kept_off.data(), ctx->h_stage, 4ull * (nm + 1));
 
     R.n_mol = nm;

@@ -69,6 +69,41 @@ struct HostDownload {
     size_t bytes = 0, vb = 0, tb = 0, ab = 0;
     unsigned long long d2h = 0;  // bytes copied
 };
+
+// Host values a pipeline segment produces besides its stream work (kept with its graph).
+struct SegOut {
+    int launches = 0;             // kernels the segment launches
+    int alt = 0;                  // which ping-pong pair holds a sort's result
+};
+
+// Launch shape of a Gauss-Seidel pass: sequential waves of wsize vertices, each a table of
+// contiguous slabs (at most smax vertices, at most qcap slabs) taken by `ctas` persistent
+// CTAs.  A function of the vertex count, the molecule count and the GsShape only.
+struct GsLaunch {
+    int ctas;
+    unsigned smax, qcap, wsize, waves;
+    unsigned table_words;  // per wave
+};
+// The plan: launch shape plus the slab tables (host words, waves x table_words), which
+// follow the molecules' vertex ranges.
+struct GsPlan {
+    GsLaunch L;
+    unsigned max_slabs = 0, max_len = 0;  // diagnostics
+    std::vector<unsigned> table;
+};
+
+// One cached segment graph: its executable, the key bytes it was captured from, the host
+// values the capture produced and when it was last used.
+struct GraphSeg {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned char> key;
+    SegOut out;
+    unsigned long long used = 0;
+};
+// Graphs kept per segment slot (a batch call split by smoothing passes alternates shapes).
+constexpr int kSegCache = 4;
+// Graph slots: per-molecule field / mesh / finish, then the batch's.
+enum { kSegField = 0, kSegMesh, kSegFinish, kSegBatchField, kSegBatchMesh, kSegBatchFinish, kSegSlots };
 }  // namespace qses
 
 struct qses_context {
@@ -76,9 +111,12 @@ struct qses_context {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaStream_t side = nullptr;          // closest atom, filter and downloads beside the smoothing
+    cudaStream_t capture = nullptr;       // private stream that pipeline segments are captured on
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     qses::HostDownload dl;
-    qses::Arena input, field, mesh_ws;
+    qses::Arena input, field, mesh_ws, gs_ws;
+    unsigned *h_gs = nullptr;         // pinned slab tables of the smoothing launches (grows)
+    size_t h_gs_cap = 0;
     void *small = nullptr;            // 4 KB device scratch: bounds, error word, queue counters
     unsigned char *h_small = nullptr; // 4 KB pinned host scratch
     QGrid grid;
@@ -99,6 +137,10 @@ struct qses_context {
     int edt_force = -1;               // autotuner: forced refine tile shape (-1 = none)
     int edt_used = 0;
     unsigned long long diag[10] = {0};  // smoothing diagnostics: slabs, slab size, max/idle/total rounds
+    bool use_graphs = true;           // pipeline segments through CUDA graphs
+    qses::GraphSeg seg[qses::kSegSlots][qses::kSegCache];
+    unsigned long long seg_clock = 0;
+    unsigned long long graph_stats[4] = {0};  // captures, instantiations, in-place updates, replays
 
     int fail(int code, const char *what, cudaError_t e = cudaSuccess);
     void mark(const char *name);
@@ -112,10 +154,26 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
 // depends on earlier, finished waves.
 // `before_writeback` (may be null): event the stream waits for before the smoothed
 // positions overwrite vq (work on another stream that still reads the welded positions).
-int run_smoothing(qses_context *ctx, const GsShape &sh, int passes, float *vq, float4 *pos4, unsigned nv,
-                  const uint2 *deg, const unsigned *nbr, unsigned short *cnt, int *remote, unsigned *inbox,
-                  unsigned *inbox_tail, int *d_err, unsigned long long *stats, bool record_slabs,
-                  cudaEvent_t before_writeback = nullptr);
+int run_smoothing(qses_context *ctx, const GsShape &sh, const GsLaunch &L, int passes, float *vq, float4 *pos4,
+                  unsigned nv, const uint2 *deg, const unsigned *nbr, unsigned short *cnt, int *remote, uint2 *home,
+                  unsigned *table, const unsigned *h_table, unsigned *inbox, unsigned *inbox_tail, int *d_err,
+                  unsigned long long *stats, cudaEvent_t before_writeback = nullptr);
+// Slab plan of a pass over nv vertices.  mol_off (nm + 1 entries, null for one molecule):
+// the molecules' vertex ranges, never split by a slab boundary unless a molecule is larger
+// than the slab size; mol_depth: a per-molecule estimate of the dependency depth (grid size),
+// which orders the slabs by when their inputs are expected.  Fills pl.table.
+int gs_plan(int device, const GsShape &sh, unsigned nv, const unsigned *mol_off, const int *mol_depth, unsigned nm,
+            GsPlan &pl);
+// The same for at most pmax resident slab CTAs (no device query).
+int gs_plan_for(int pmax, const GsShape &sh, unsigned nv, const unsigned *mol_off, const int *mol_depth, unsigned nm,
+                GsPlan &pl);
+// The smoothing workspace of a plan (home records, slab tables, inboxes) in ctx->gs_ws and
+// the plan's tables in ctx->h_gs.  Returns QSES_OK or an error code (ctx->fail called).
+struct GsBuffers {
+    uint2 *home;
+    unsigned *table, *inbox, *inbox_tail;
+};
+int gs_buffers(qses_context *ctx, const GsPlan &pl, unsigned nv, GsBuffers &out);
 // All items share `passes`; the weld keys of every item fit `key_bits` bits and
 // key_bits + bits(count - 1) <= 64.  Results in ctx->batch.
 int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int passes, int key_bits);
