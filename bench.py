@@ -448,6 +448,8 @@ def run_served_form(args):
     reqs = q.molecules.served_stream(per_rate * len(rates) + 64)
     rng = np.random.default_rng(11)
     sweep = []
+    with q.Context(0) as tctx:  # launch-shape tuning on a sample (process-wide, like a service start)
+        tune = tctx.autotune_batch(reqs[-64:-32])
     with q.Server(lanes=args.lanes, memory_budget=120 << 30, max_batch=256) as srv:
         for r in reqs[-64:]:  # warm-up: workspaces and pinned blocks grow to size once
             srv.wait(srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"]))
@@ -496,7 +498,8 @@ def run_served_form(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": "open-loop Poisson, %d requests per offered rate, atom counts log-uniform in "
                                "[200, 200000], voxel one of {0.3, 0.4, 0.5} A, 1 pass" % per_rate,
-                   "form": "served", "lanes": args.lanes, "memory_budget_gb": 120},
+                   "form": "served", "lanes": args.lanes, "memory_budget_gb": 120,
+                   "smoothing_shape": {"threads": tune[0], "slab_target": tune[1], "cache_flags": tune[2]}},
         "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "sweep": sweep, "server": stats,
         "plain_path": {"value": plain, "unit": "molecules/s",
                        "path": "the first %d requests one by one through qses_compute on the same GPU" % len(sample)},

@@ -245,6 +245,13 @@ QSES_API unsigned long long qses_last_download_bytes(qses_context *ctx);
  * warps).  Returns the number of values written. */
 QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max);
 
+/* Host timeline of the last pipeline run on ctx (ms; for a batch call, its last batch):
+ * [0] host work before the first launch, [1] field segment from launch to its read-back,
+ * [2] host work between, [3] mesh segment, [4] host work between, [5] finish segment
+ * (closest atom, filter, smoothing, downloads).  No reference counterpart.  Returns the
+ * number of values written. */
+QSES_API int qses_host_timeline(qses_context *ctx, double *ms, int max);
+
 /* ------------------------------------------------------------------ CUDA graphs */
 
 /* No reference counterpart (QuickSES launches every kernel from the host, slice by slice).

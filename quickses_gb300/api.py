@@ -225,6 +225,14 @@ class Context:
         """Run the pipeline segments through CUDA graphs (default) or launch every kernel directly."""
         self._check(self._lib.qses_set_graphs(self._h, int(bool(enable))), "qses_set_graphs")
 
+    def host_timeline(self):
+        """Host timeline of the last pipeline run (ms): before the first launch, field segment,
+        gap, mesh segment, gap, finish segment."""
+        out = (ctypes.c_double * 6)()
+        k = self._lib.qses_host_timeline(self._h, out, 6)
+        names = ["host_prep", "field", "host_mid1", "mesh", "host_mid2", "finish"]
+        return {names[q]: float(out[q]) for q in range(k)}
+
     def graph_stats(self):
         out = (ctypes.c_ulonglong * 4)()
         k = self._lib.qses_graph_stats(self._h, out, 4)

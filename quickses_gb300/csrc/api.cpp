@@ -701,6 +701,13 @@ QSES_API int qses_debug_slab_plan(unsigned nv, const unsigned *mol_off, const in
     return QSES_OK;
 }
 
+QSES_API int qses_host_timeline(qses_context *ctx, double *ms, int max) {
+    if (!ctx || !ms) return 0;
+    int k = 0;
+    for (; k < max && k < 6; k++) ms[k] = ctx->timeline[k];
+    return k;
+}
+
 QSES_API int qses_set_graphs(qses_context *ctx, int enable) {
     if (!ctx) return QSES_ERR_INVALID_ARG;
     ctx->use_graphs = enable != 0;

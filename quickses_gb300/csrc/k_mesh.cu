@@ -502,14 +502,17 @@ __global__ void k_tri_compact_batch(QBatch b, const unsigned *__restrict__ tri, 
 
 // --------------------------------------------------------------- smoothing
 
-__global__ void k_degree(const unsigned *__restrict__ tri, size_t n3, unsigned nv, uint2 *__restrict__ deg) {
-    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < n3) atomicAdd(&deg[tri[q]].x, 2u);
-}
-
-__global__ void k_copy_keys(const unsigned *__restrict__ tri, size_t n3, unsigned *__restrict__ keys) {
-    size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < n3) keys[q] = tri[q];
+// Neighbour-list offsets from the stably sorted corner occurrences: v's list starts at twice
+// the position of its first occurrence (two entries per occurrence); vertices between two
+// sorted keys (none in a welded mesh) get empty lists.
+__global__ void k_csr_offsets(const unsigned *__restrict__ skey, size_t n3, unsigned nv, uint2 *__restrict__ start) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n3) return;
+    const unsigned k = skey[p];
+    const long long prev = p ? (long long)skey[p - 1] : -1ll;
+    for (long long v = prev + 1; v <= (long long)k && v <= (long long)nv; v++) start[v] = make_uint2(2u * (unsigned)p, 0u);
+    if (p == n3 - 1)
+        for (long long v = (long long)k + 1; v <= (long long)nv; v++) start[v] = make_uint2(2u * (unsigned)n3, 0u);
 }
 
 // Sorted occurrence p (vertex v, corner q = 3t + c in triangle order) contributes the two
@@ -632,7 +635,7 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // vertices.  Table: Q, the Q + 1 slab bounds in id order (qcap + 1 slots), then the Q slab ids
 // in the order they are taken.
 template <int kGsT, unsigned kFlags>
-__global__ void __launch_bounds__(kGsT, 1) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned smax,
+__global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned smax,
                                                   const unsigned *__restrict__ table, unsigned qcap,
                                                   unsigned *next_slab, const uint2 *__restrict__ home,
                                                   const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
@@ -970,11 +973,8 @@ void launch_tri_flags(const unsigned *tri, unsigned nt, uint2 *flags, cudaStream
 void launch_tri_compact(const unsigned *tri, unsigned nt, const uint2 *excl, unsigned *out, cudaStream_t s) {
     k_tri_compact<<<nblk(nt, 256), 256, 0, s>>>(tri, nt, excl, out);
 }
-void launch_degree(const unsigned *tri, size_t n3, unsigned nv, uint2 *deg, cudaStream_t s) {
-    k_degree<<<nblk(n3, 256), 256, 0, s>>>(tri, n3, nv, deg);
-}
-void launch_copy_keys(const unsigned *tri, size_t n3, unsigned *keys, cudaStream_t s) {
-    k_copy_keys<<<nblk(n3, 256), 256, 0, s>>>(tri, n3, keys);
+void launch_csr_offsets(const unsigned *skey, size_t n3, unsigned nv, uint2 *start, cudaStream_t s) {
+    k_csr_offsets<<<nblk(n3, 256), 256, 0, s>>>(skey, n3, nv, start);
 }
 void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s) {
     k_csr_fill<<<nblk(n3, 256), 256, 0, s>>>(tri, socc, n3, nbr);

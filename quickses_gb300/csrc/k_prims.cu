@@ -216,7 +216,8 @@ size_t radix_sort_tmp_bytes(unsigned n, int bits) {
 
 template <typename K>
 cudaError_t radix_sort(K *keys, K *keys_alt, unsigned *vals, unsigned *vals_alt, unsigned n, int bits,
-                       bool identity, void *tmp, int *d_err, cudaStream_t s, int *launches, int *in_alt) {
+                       bool identity, void *tmp, int *d_err, cudaStream_t s, int *launches, int *in_alt,
+                       const K *keys_in) {
     *in_alt = 0;
     int npass = (bits + 7) / 8;
     if (npass > (int)sizeof(K)) npass = (int)sizeof(K);
@@ -231,9 +232,11 @@ cudaError_t radix_sort(K *keys, K *keys_alt, unsigned *vals, unsigned *vals_alt,
     if (e != cudaSuccess) return e;
     unsigned hblocks = (n + 255) / 256;
     if (hblocks > 1216) hblocks = 1216;
-    k_rs_hist<K><<<hblocks, 256, 0, s>>>(keys, n, npass, hist);
+    const K *first = keys_in ? keys_in : keys;
+    k_rs_hist<K><<<hblocks, 256, 0, s>>>(first, n, npass, hist);
     if (launches) (*launches)++;
-    K *src = keys, *dst = keys_alt;
+    const K *src = first;
+    K *dst = keys_alt, *other = keys;  // passes after the first ping-pong between keys_alt and keys
     unsigned *vsrc = identity ? nullptr : vals, *vdst = vals_alt;
     for (int p = 0; p < npass; p++) {
         e = cudaMemsetAsync(ticket, 0, 256, s);
@@ -243,7 +246,8 @@ cudaError_t radix_sort(K *keys, K *keys_alt, unsigned *vals, unsigned *vals_alt,
         if (launches) (*launches)++;
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        K *tk = src; src = dst; dst = tk;
+        src = dst;
+        K *tk = other; other = dst; dst = tk;
         unsigned *written = vdst;
         vdst = (written == vals_alt) ? vals : vals_alt;
         vsrc = written;
@@ -253,9 +257,9 @@ cudaError_t radix_sort(K *keys, K *keys_alt, unsigned *vals, unsigned *vals_alt,
 }
 
 template cudaError_t radix_sort<unsigned>(unsigned *, unsigned *, unsigned *, unsigned *, unsigned, int, bool,
-                                          void *, int *, cudaStream_t, int *, int *);
+                                          void *, int *, cudaStream_t, int *, int *, const unsigned *);
 template cudaError_t radix_sort<unsigned long long>(unsigned long long *, unsigned long long *, unsigned *,
                                                     unsigned *, unsigned, int, bool, void *, int *, cudaStream_t,
-                                                    int *, int *);
+                                                    int *, int *, const unsigned long long *);
 
 }  // namespace qses

@@ -125,7 +125,9 @@ static int tune_bucket(unsigned nv) { return bits_for(nv); }
 GsShape gs_shape(unsigned nv, bool batch) {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     const int b = tune_bucket(nv);
-    return g_tuned[batch][b] ? g_tune[batch][b] : GsShape();
+    if (g_tuned[batch][b]) return g_tune[batch][b];
+    // untuned: the shapes the tuner picks on balls of 1 000 - 50 000 atoms and on batches
+    return batch ? GsShape{1024, 25000, kGsL1Positions, 0} : GsShape{1024, 4096, kGsL1Positions, 0};
 }
 
 void gs_shape_record(unsigned nv, bool batch, GsShape sh) {
@@ -151,7 +153,7 @@ void edt_shape_record(int G, int shape) {
 }
 
 int gs_shape_candidates(GsShape *out, int max) {
-    static const unsigned targets[] = {4096, 16384, 25000};
+    static const unsigned targets[] = {4096, 8192, 16384, 25000};
     // the persisting-L2 window (kGsPersistL2) is left to callers that force it: it changes
     // stream attributes (its segment then runs outside CUDA graphs) and its reset after the
     // pass costs more than the pass gains
@@ -215,7 +217,11 @@ static unsigned ceil_div(unsigned long long a, unsigned long long b) { return (u
 
 int gs_plan(int device, const GsShape &sh, unsigned nv, const unsigned *mol_off, const int *mol_depth, unsigned nm,
             GsPlan &pl) {
-    const int pmax = std::min(gs_slab_max_blocks(device, kGsSlabMaxVerts, sh.threads), 1024);
+    // resident slab CTAs: one molecule's slabs may hold up to the largest slab; a batch's at
+    // most the target, so smaller targets fit more CTAs per SM
+    const bool single = mol_off == nullptr || nm <= 1;
+    const unsigned smax = single ? kGsSlabMaxVerts : std::min(std::max(sh.target, 256u), kGsSlabMaxVerts);
+    const int pmax = std::min(gs_slab_max_blocks(device, smax, sh.threads), 1024);
     if (pmax < 1) return QSES_ERR_NO_DEVICE;
     return gs_plan_for(pmax, sh, nv, mol_off, mol_depth, nm, pl);
 }
@@ -245,10 +251,11 @@ int gs_plan_for(int pmax, const GsShape &sh, unsigned nv, const unsigned *mol_of
             L.qcap = std::max(L.qcap, pieces(nw));
         }
     } else {
-        // split molecules: at most len / t + 1 slabs each; packed runs of small molecules: at most
-        // 2 (run / t) + 1 (two neighbouring packed slabs hold more than t)
-        L.qcap = 2 * ceil_div(L.wsize, t) + 2 * nm + 2;
-        L.smax = Smax;
+        // split molecules: ceil(len / t) slabs of at most t each (at most len / t + 1); packed
+        // runs of small molecules: at most 2 (run / t) + 1 (two neighbouring packed slabs hold
+        // more than t), and at most one run more than there are split molecules
+        L.qcap = 3 * ceil_div(L.wsize, t) + 2 * nm + 2;
+        L.smax = t;
     }
     L.ctas = (int)std::min<unsigned>((unsigned)pmax, L.qcap);
     L.table_words = (unsigned)gs_table_words(L.qcap);
@@ -265,7 +272,7 @@ int gs_plan_for(int pmax, const GsShape &sh, unsigned nv, const unsigned *mol_of
         const unsigned v0 = w * L.wsize, v1 = std::min(nv, v0 + L.wsize);
         slabs.clear();
         auto split = [&](unsigned s0, unsigned s1, int depth) {
-            const unsigned len = s1 - s0, k = pieces(len), S = ceil_div(len, k);
+            const unsigned len = s1 - s0, k = single ? pieces(len) : ceil_div(len, t), S = ceil_div(len, k);
             for (unsigned a = s0; a < s1; a += S)
                 slabs.push_back({a, std::min(s1, a + S), (float)((double)(a - s0) / len * depth), depth});
         };
@@ -522,25 +529,27 @@ static int enqueue_finish(qses_context *ctx, const FinishSeg &c, SegOut &o) {
     }
     ctx->mark("filter");
     const unsigned *tri_out = c.keep_all ? c.tri : c.tri_kept;
-    if (c.h_dl) {
-        if (c.dl_tb) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb, tri_out, c.dl_tb, cudaMemcpyDeviceToHost, sd));
-        if (c.dl_ab) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb, c.asorted, c.dl_ab, cudaMemcpyDeviceToHost, sd));
+    // triangles and atom ids to the host: beside the smoothing when forked, else (stage
+    // timing) in the download stage
+    auto download_rest = [&](cudaStream_t q) -> int {
+        if (c.dl_tb) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb, tri_out, c.dl_tb, cudaMemcpyDeviceToHost, q));
+        if (c.dl_ab) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb, c.asorted, c.dl_ab, cudaMemcpyDeviceToHost, q));
         if (c.dl_ab)
-            QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb + c.dl_ab, c.ainput, c.dl_ab, cudaMemcpyDeviceToHost, sd));
-    }
+            QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb + c.dl_ab, c.ainput, c.dl_ab, cudaMemcpyDeviceToHost, q));
+        return QSES_OK;
+    };
+    if (c.h_dl && c.fork) QCHK_RC(download_rest(sd));
     if (c.fork) QCHK(cudaEventRecord(ctx->ev_join, sd));
 
     // Gauss-Seidel smoothing on the device
     if (c.passes > 0 && c.nv > 0 && c.nt > 0) {
-        QCHK(cudaMemsetAsync(c.deg, 0, 8ull * (c.nv + 1), s));
-        launch_degree(c.tri, c.n3, c.nv, c.deg, s);
-        ctx->launches++;
-        QCHK(scan_u2(c.deg, c.deg, c.nv + 1, nullptr, c.tmpb, c.err, s, &ctx->launches));
-        launch_copy_keys(c.tri, c.n3, c.okey, s);
-        ctx->launches++;
+        // neighbour lists: the 3T corners stably sorted by vertex (the triangle order within a
+        // vertex is the order getNeighboorsVertices appends in), offsets from the sorted keys
         QCHK(radix_sort<unsigned>(c.okey, c.okey2, c.oval, c.oval2, (unsigned)c.n3, bits_for(c.nv - 1), true, c.tmpb,
-                                  c.err, s, &ctx->launches, &o.alt));
-        const unsigned *socc = o.alt ? c.oval2 : c.oval;
+                                  c.err, s, &ctx->launches, &o.alt, c.tri));
+        const unsigned *socc = o.alt ? c.oval2 : c.oval, *skey = o.alt ? c.okey2 : c.okey;
+        launch_csr_offsets(skey, c.n3, c.nv, c.deg, s);
+        ctx->launches++;
         launch_csr_fill(c.tri, socc, c.n3, c.nbr, s);
         ctx->launches++;
         ctx->mark("smooth_csr");
@@ -552,6 +561,7 @@ static int enqueue_finish(qses_context *ctx, const FinishSeg &c, SegOut &o) {
     }
     ctx->mark("smooth");
     if (c.h_dl && c.dl_vb) QCHK(cudaMemcpyAsync(c.h_dl, c.vq, c.dl_vb, cudaMemcpyDeviceToHost, s));
+    if (c.h_dl && !c.fork) QCHK_RC(download_rest(s));
     if (c.fork) QCHK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     QCHK(cudaMemcpyAsync(c.h_out + 8, c.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     QCHK(cudaMemcpyAsync(c.h_out + 2048, c.stats, 64, cudaMemcpyDeviceToHost, s));
@@ -560,6 +570,8 @@ static int enqueue_finish(qses_context *ctx, const FinishSeg &c, SegOut &o) {
 
 int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n) {
     cudaStream_t s = ctx->stream;
+    memset(ctx->timeline, 0, sizeof(ctx->timeline));
+    ctx->tick(-1);
     ctx->launches = 0;
     for (auto &m : ctx->marks) cudaEventDestroy(m.second);
     ctx->marks.clear();
@@ -638,9 +650,11 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     if (!a.tmp) return ctx->fail(QSES_ERR_INTERNAL, "field workspace layout");
     fill_lut(g, (float *)(ctx->h_small + 64));
     SegOut oa;
+    ctx->tick(0);
     QCHK_RC(run_segment(ctx, kSegField, a, oa, enqueue_field));
     unsigned *skey = oa.alt ? a.key2 : a.key, *sidx = oa.alt ? a.idx2 : a.idx;
     QCHK(cudaStreamSynchronize(s));
+    ctx->tick(1);
     ctx->mark("mc_count");
     uint2 tot;
     memcpy(&tot, ctx->h_small, sizeof(tot));
@@ -707,6 +721,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     b.key_bits = key_bits;
     b.g = g;
     SegOut ob;
+    ctx->tick(2);
     QCHK_RC(run_segment(ctx, kSegMesh, b, ob, enqueue_mesh));
     unsigned nv = 0;
     if (NE > 0) {
@@ -714,6 +729,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         memcpy(&tot, ctx->h_small, sizeof(tot));
         nv = tot.x;
     }
+    ctx->tick(3);
     ctx->mark("weld");
 
     // Closest atom, degenerate filter and (for host results) the triangle and atom-id
@@ -787,9 +803,11 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     }
     c.g = g;
     SegOut oc;
+    ctx->tick(4);
     // an L2 persistence window is a stream attribute, set when the launch is enqueued
     QCHK_RC(run_segment(ctx, kSegFinish, c, oc, enqueue_finish, !(smoothing && (c.sh.flags & kGsPersistL2))));
     QCHK(cudaStreamSynchronize(s));
+    ctx->tick(5);
     ctx->mark("download");
     memcpy(ctx->diag + 2, ctx->h_small + 2048, 7 * sizeof(unsigned long long));
     unsigned nkept = T;
@@ -834,6 +852,12 @@ int qses_context::fail(int code, const char *what, cudaError_t e) {
         snprintf(buf, sizeof(buf), "%s: %s", qses_status_string(code), what);
     last_error = buf;
     return code;
+}
+
+void qses_context::tick(int k) {
+    const auto now = std::chrono::steady_clock::now();
+    if (k >= 0 && k < 6) timeline[k] = std::chrono::duration<double, std::milli>(now - tl_last).count();
+    tl_last = now;
 }
 
 void qses_context::mark(const char *name) {

@@ -234,25 +234,27 @@ static int enqueue_batch_finish(qses_context *ctx, const BatchFinishSeg &c, SegO
     QCHK(cudaMemcpyAsync(c.h_out, c.tot, sizeof(uint2), cudaMemcpyDeviceToHost, sd));
     QCHK(cudaMemcpyAsync(c.h_kept, c.kept_off, 4ull * (nm + 1), cudaMemcpyDeviceToHost, sd));
     ctx->mark("filter");
-    if (c.h_dl) {
-        if (c.dl_tb) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb, c.tri_kept, c.dl_tb, cudaMemcpyDeviceToHost, sd));
-        if (c.dl_ab) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb, c.asorted, c.dl_ab, cudaMemcpyDeviceToHost, sd));
+    // triangles and atom ids to the host: beside the smoothing when forked, else (stage
+    // timing) in the download stage
+    auto download_rest = [&](cudaStream_t q) -> int {
+        if (c.dl_tb) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb, c.tri_kept, c.dl_tb, cudaMemcpyDeviceToHost, q));
+        if (c.dl_ab) QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb, c.asorted, c.dl_ab, cudaMemcpyDeviceToHost, q));
         if (c.dl_ab)
-            QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb + c.dl_ab, c.ainput, c.dl_ab, cudaMemcpyDeviceToHost, sd));
-    }
+            QCHK(cudaMemcpyAsync(c.h_dl + c.dl_vb + c.dl_tb + c.dl_ab, c.ainput, c.dl_ab, cudaMemcpyDeviceToHost, q));
+        return QSES_OK;
+    };
+    if (c.h_dl && c.fork) QCHK_RC(download_rest(sd));
     if (c.fork) QCHK(cudaEventRecord(ctx->ev_join, sd));
 
     // Gauss-Seidel over all molecules
     if (c.passes > 0 && c.nv > 0 && c.nt > 0) {
-        QCHK(cudaMemsetAsync(c.deg, 0, 8ull * (c.nv + 1), s));
-        launch_degree(c.tri, c.n3, c.nv, c.deg, s);
-        ctx->launches++;
-        QCHK(scan_u2(c.deg, c.deg, c.nv + 1, nullptr, c.tmpb, c.err, s, &ctx->launches));
-        launch_copy_keys(c.tri, c.n3, c.okey, s);
-        ctx->launches++;
+        // neighbour lists: the 3T corners stably sorted by vertex (the triangle order within a
+        // vertex is the order getNeighboorsVertices appends in), offsets from the sorted keys
         QCHK(radix_sort<unsigned>(c.okey, c.okey2, c.oval, c.oval2, (unsigned)c.n3, bits_for(c.nv - 1), true, c.tmpb,
-                                  c.err, s, &ctx->launches, &o.alt));
-        const unsigned *socc = o.alt ? c.oval2 : c.oval;
+                                  c.err, s, &ctx->launches, &o.alt, c.tri));
+        const unsigned *socc = o.alt ? c.oval2 : c.oval, *skey = o.alt ? c.okey2 : c.okey;
+        launch_csr_offsets(skey, c.n3, c.nv, c.deg, s);
+        ctx->launches++;
         launch_csr_fill(c.tri, socc, c.n3, c.nbr, s);
         ctx->launches++;
         ctx->mark("smooth_csr");
@@ -264,6 +266,7 @@ static int enqueue_batch_finish(qses_context *ctx, const BatchFinishSeg &c, SegO
     }
     ctx->mark("smooth");
     if (c.h_dl && c.dl_vb) QCHK(cudaMemcpyAsync(c.h_dl, c.vq, c.dl_vb, cudaMemcpyDeviceToHost, s));
+    if (c.h_dl && !c.fork) QCHK_RC(download_rest(s));
     if (c.fork) QCHK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     QCHK(cudaMemcpyAsync(c.h_out + 8, c.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     return QSES_OK;
@@ -271,6 +274,8 @@ static int enqueue_batch_finish(qses_context *ctx, const BatchFinishSeg &c, SegO
 
 int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int passes, int key_bits) {
     cudaStream_t s = ctx->stream;
+    memset(ctx->timeline, 0, sizeof(ctx->timeline));
+    ctx->tick(-1);
     ctx->launches = 0;
     for (auto &m : ctx->marks) cudaEventDestroy(m.second);
     ctx->marks.clear();
@@ -418,10 +423,12 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     a.units = (unsigned)units;
     a.cell_bits = cell_bits;
     SegOut oa;
+    ctx->tick(0);
     QCHK_RC(run_segment(ctx, kSegBatchField, a, oa, enqueue_batch_field));
     const unsigned *sidx = oa.alt ? a.idx2 : a.idx;
     unsigned *hsm = (unsigned *)ctx->h_small;  // 4 KB pinned: totals and the error word
     QCHK(cudaStreamSynchronize(s));
+    ctx->tick(1);
     ctx->mark("mc_count");
     if (hsm[2]) return ctx->fail((int)hsm[2], "device wait in the batch field stage");
     const unsigned T = hsm[0], NE = hsm[1];
@@ -487,8 +494,10 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     mb.tot_bits = tot_bits;
     mb.b = b;
     SegOut ob;
+    ctx->tick(2);
     QCHK_RC(run_segment(ctx, kSegBatchMesh, mb, ob, enqueue_batch_mesh));
     QCHK(cudaStreamSynchronize(s));
+    ctx->tick(3);
     std::vector<unsigned> vtx_off(nm + 1);
     memcpy(vtx_off.data(), ctx->h_stage, 4ull * (nm + 1));
     const unsigned nv = NE > 0 ? hsm[0] : 0;
@@ -570,9 +579,11 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     }
     c.b = b;
     SegOut oc;
+    ctx->tick(4);
     // an L2 persistence window is a stream attribute, set when the launch is enqueued
     QCHK_RC(run_segment(ctx, kSegBatchFinish, c, oc, enqueue_batch_finish, !(smoothing && (c.sh.flags & kGsPersistL2))));
     QCHK(cudaStreamSynchronize(s));
+    ctx->tick(5);
     ctx->mark("download");
     if (hsm[2]) return ctx->fail((int)hsm[2], "device wait in the batch mesh stage");
     const unsigned nkept = hsm[0];

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <string>
 #include <utility>
 #include <vector>
@@ -141,6 +142,11 @@ struct qses_context {
     qses::GraphSeg seg[qses::kSegSlots][qses::kSegCache];
     unsigned long long seg_clock = 0;
     unsigned long long graph_stats[4] = {0};  // captures, instantiations, in-place updates, replays
+    // host timeline of the last pipeline call (ms): host work before the first launch, field
+    // segment (launch to read-back), host gap, mesh segment, host gap, finish segment
+    double timeline[6] = {0};
+    void tick(int k);                 // closes timeline interval k at "now"
+    std::chrono::steady_clock::time_point tl_last;
 
     int fail(int code, const char *what, cudaError_t e = cudaSuccess);
     void mark(const char *name);

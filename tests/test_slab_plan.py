@@ -36,12 +36,14 @@ def _plan(nv, mol_off=None, depth=None, threads=1024, target=16384, wave=0, pmax
         t = table[w * words:(w + 1) * words]
         Q = int(t[0])
         out.append((np.array(t[1:Q + 2], np.int64), np.array(t[qcap + 2:qcap + 2 + Q], np.int64)))
-    return dict(ctas=ctas, smax=smax, qcap=qcap, wsize=wsize, waves=waves), out
+    return dict(ctas=ctas, smax=smax, qcap=qcap, wsize=wsize, waves=waves, target=target), out
 
 
 def _check(nv, mol_off, info, waves, pmax=152):
     mol_off = np.array([0, nv] if mol_off is None else mol_off, np.int64)
     assert info["ctas"] == min(pmax, info["qcap"]) and info["smax"] <= SMAX
+    if mol_off is not None and len(mol_off) > 2:
+        assert info["smax"] <= max(256, min(info["target"], SMAX))
     v0 = 0
     for bnd, order in waves:
         Q = len(order)
