@@ -412,6 +412,7 @@ def run_batch_form(args):
                 times.append(time.perf_counter() - t0)
         sec = float(np.mean(times))
         graphs_timed = ctx.graph_stats()
+        timeline = ctx.host_timeline()
         _raw_single(lib, L, ctx, reqs[:8])
         t0 = time.perf_counter()
         _raw_single(lib, L, ctx, reqs)
@@ -433,6 +434,8 @@ def run_batch_form(args):
         "plain_path": {"value": n / t_plain, "unit": "molecules/s",
                        "path": "the same molecules one by one through qses_compute on the same GPU"},
         "stages_ms": {k: round(v, 3) for k, v in stages}, "gpu_launches": launches * args.steps,
+        "step_ms": [round(1e3 * t, 3) for t in times],
+        "host_timeline_ms": {k: round(v, 3) for k, v in timeline.items()},
         "clocks": clk.summary()}))
 
 

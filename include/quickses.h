@@ -178,9 +178,10 @@ QSES_API int qses_set_field_shape(qses_context *ctx, int shape);
 /* Fixes the smoothing launch shape of ctx: threads 512 or 1024 per slab CTA, slab size
  * aimed at (>= 256 vertices), cache_flags bit 0 = prefetch successors' neighbour lists into
  * L1 instead of L2, bit 1 = neighbour positions through L1, bit 2 = keep the positions in
- * persisting L2 lines during the pass (a window on the context's stream, cleared after it);
- * wave_vertices = most vertices per slab-kernel launch (0 = as many as fit: 152 SMs x 25 000;
- * larger meshes run as sequential waves); threads = 0 returns to the tuned/default shape.
+ * persisting L2 lines during the pass (a window on the context's stream, cleared after it),
+ * bit 3 = each slab's own positions in shared memory (slabs of at most 8192 vertices);
+ * wave_vertices = most vertices per slab-kernel launch (0 = the whole mesh in one launch;
+ * otherwise sequential waves); threads = 0 returns to the tuned/default shape.
  * Every shape gives the same mesh. */
 QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags,
                                       unsigned wave_vertices);
@@ -241,8 +242,8 @@ QSES_API unsigned long long qses_last_download_bytes(qses_context *ctx);
 /* Smoothing diagnostics of the last call: [0] slabs, [1] vertices per slab, [2] most
  * boundary polls of one slab, [3] slabs that did not finish, [4] clock cycles spent in
  * vertex updates, [5] in releasing successors, [6] vertices updated, [7] cycles until a
- * vertex's neighbour ids arrived, [8] then until their positions arrived (summed over
- * warps).  Returns the number of values written. */
+ * vertex's neighbour ids arrived, [8] then until their positions arrived, [9] in the
+ * position store and its fence (summed over warps).  Returns the number of values written. */
 QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max);
 
 /* Host timeline of the last pipeline run on ctx (ms; for a batch call, its last batch):
@@ -322,13 +323,14 @@ QSES_API int qses_debug_codes(qses_context *ctx, uint8_t *codes, size_t bytes);
 QSES_API int qses_debug_atom_order(qses_context *ctx, uint32_t *sorted_to_input, uint32_t *hash, unsigned n);
 /* Slab plan of the smoothing pass, for tests (no reference counterpart, no GPU needed): nv
  * vertices, molecules' vertex ranges mol_off (nm + 1 entries; NULL = one molecule) and
- * depth estimates, smoothing shape (threads, target, wave as qses_set_smoothing_shape) and
+ * depth estimates, smoothing shape (threads, target, cache_flags, wave as
+ * qses_set_smoothing_shape) and
  * pmax resident slab CTAs.  launch[0..5] = ctas, smax, qcap, wsize, waves, words per wave;
  * table (cap words): the waves' slab tables [Q, Q + 1 bounds (qcap + 1 slots), Q slab ids in
  * the order CTAs take them].  Returns QSES_OK or an error code. */
 QSES_API int qses_debug_slab_plan(unsigned nv, const unsigned *mol_off, const int *depth, unsigned nm, int threads,
-                                  unsigned target, unsigned wave, int pmax, unsigned *launch, unsigned *table,
-                                  size_t cap);
+                                  unsigned target, unsigned cache_flags, unsigned wave, int pmax, unsigned *launch,
+                                  unsigned *table, size_t cap);
 
 /* --------------------------------------------------------- synthetic molecules */
 QSES_API int qses_synth_ball(unsigned N, uint64_t seed, float density, float min_dist, float *xyz,

@@ -108,7 +108,7 @@ SIGNATURES = {
     "qses_set_graphs": (ctypes.c_int, [_VP, ctypes.c_int]),
     "qses_host_timeline": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "qses_debug_slab_plan": (ctypes.c_int, [ctypes.c_uint, _VP, _VP, ctypes.c_uint, ctypes.c_int, ctypes.c_uint,
-                                            ctypes.c_uint, ctypes.c_int, _VP, _VP, ctypes.c_size_t]),
+                                            ctypes.c_uint, ctypes.c_uint, ctypes.c_int, _VP, _VP, ctypes.c_size_t]),
     "qses_graph_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
     "qses_field_codes_noalloc": (ctypes.c_int, [_VP, _VP, ctypes.c_uint, ctypes.c_float, _VP, ctypes.c_size_t,
                                                 _VP]),

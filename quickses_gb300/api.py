@@ -243,7 +243,7 @@ class Context:
         out = (ctypes.c_ulonglong * 10)()
         k = self._lib.qses_diagnostics(self._h, out, 10)
         names = ["slabs", "slab_size", "max_polls", "unfinished_slabs", "update_cycles", "release_cycles",
-                 "vertices", "id_wait_cycles", "position_wait_cycles"]
+                 "vertices", "id_wait_cycles", "position_wait_cycles", "store_fence_cycles"]
         return {names[q]: int(out[q]) for q in range(min(k, len(names)))}
 
 

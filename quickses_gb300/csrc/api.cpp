@@ -32,6 +32,8 @@ struct HostMesh {
     std::atomic<int> *refs = nullptr;  // shared block of a batch: the last release returns it
 };
 
+std::atomic<unsigned long long> g_pinned_frees{0};
+
 class PinnedPool {
   public:
     // Returns a block of at least `bytes` (rounded up to a size class), or nullptr.
@@ -77,6 +79,7 @@ class PinnedPool {
                 return;
             }
         }
+        g_pinned_frees++;
         cudaFreeHost(p);
     }
 
@@ -104,6 +107,7 @@ class PinnedPool {
     void trim(size_t keep) {
         std::lock_guard<std::mutex> lock(mu_);
         while (cached_ > keep && !free_.empty()) {
+            g_pinned_frees++;
             cudaFreeHost(free_.back().first);
             cached_ -= free_.back().second;
             free_.pop_back();
@@ -123,6 +127,7 @@ PinnedPool &pinned_pool() {
 
 void *qses::pinned_take(size_t bytes, size_t *got) { return pinned_pool().take(bytes, got); }
 void qses::pinned_give(void *p, size_t bytes) { pinned_pool().give(p, bytes); }
+unsigned long long qses::pinned_frees() { return g_pinned_frees.load(); }
 
 namespace {
 
@@ -518,7 +523,7 @@ QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned t
         ctx->gs_force = qses::GsShape{0, 0, 0, 0};
         return QSES_OK;
     }
-    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 7 ||
+    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 15 ||
         (wave_vertices != 0 && wave_vertices < target))
         return QSES_ERR_INVALID_ARG;
     ctx->gs_force = qses::GsShape{threads, target, cache_flags, wave_vertices};
@@ -686,11 +691,12 @@ QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int ma
 }
 
 QSES_API int qses_debug_slab_plan(unsigned nv, const unsigned *mol_off, const int *depth, unsigned nm, int threads,
-                                  unsigned target, unsigned wave, int pmax, unsigned *launch, unsigned *table,
-                                  size_t cap) {
+                                  unsigned target, unsigned cache_flags, unsigned wave, int pmax, unsigned *launch,
+                                  unsigned *table, size_t cap) {
     if (!launch || (nm > 1 && !mol_off)) return QSES_ERR_INVALID_ARG;
     qses::GsPlan pl;
-    const int rc = qses::gs_plan_for(pmax, qses::GsShape{threads, target, 0, wave}, nv, mol_off, depth, nm, pl);
+    const int rc =
+        qses::gs_plan_for(pmax, qses::GsShape{threads, target, cache_flags, wave}, nv, mol_off, depth, nm, pl);
     if (rc != QSES_OK) return rc;
     const unsigned v[6] = {(unsigned)pl.L.ctas, pl.L.smax, pl.L.qcap, pl.L.wsize, pl.L.waves, pl.L.table_words};
     memcpy(launch, v, sizeof(v));

@@ -540,6 +540,10 @@ __device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
 // through global memory (an acquire/release counter per vertex and a per-slab inbox).
 // Each vertex is still computed exactly as the sequential loop would.
 constexpr int kGsSlabMaxSmem = 200 * 1024;  // dynamic part: offsets, packed counters, ring: 8 B/vertex
+                                            // (+ 16 B/vertex of positions with kGsSmemPos)
+__host__ __device__ constexpr size_t gs_spos_offset(unsigned smax) {
+    return ((4ull * (smax + 1) + 4ull * ((smax + 1) / 2) + 2ull * smax) + 15) & ~(size_t)15;
+}
 
 // Per vertex: lower-id neighbour entries inside its slab (+1 if any lie in lower slabs),
 // the count of entries in lower slabs, and its home: slab id and the slab's first vertex.
@@ -648,11 +652,15 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
     unsigned *st = s_dyn;                                        // len + 1 CSR offsets of the slab
     unsigned *cnt = s_dyn + (smax + 1);                          // (len + 1) / 2 words: packed counters
     volatile unsigned short *ring = (volatile unsigned short *)(cnt + (smax + 1) / 2);  // slab offsets
+    // kGsSmemPos: the slab's positions (old until a vertex updates, then new), so neighbours
+    // inside the slab are read from shared memory; others from global memory as before
+    constexpr bool kSP = (kFlags & kGsSmemPos) != 0;
+    float4 *spos = (float4 *)((char *)s_dyn + gs_spos_offset(smax));
     volatile unsigned *ob = s_ob;
     const unsigned Q = min(__ldg(table), qcap);
     const unsigned *bnd = table + 1, *order = table + 2 + qcap;
     const unsigned lane = threadIdx.x & 31;
-    unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0, cyc_ids = 0, cyc_pos = 0;
+    unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0, cyc_ids = 0, cyc_pos = 0, cyc_fence = 0;
     if (threadIdx.x == 0) s_stop = 0;
     for (;;) {
     if (threadIdx.x == 0) {
@@ -672,6 +680,8 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
     for (unsigned k = threadIdx.x; k < kGsOutbox; k += kGsT) s_ob[k] = 0xffffffffu;
     for (unsigned k = threadIdx.x; k <= len; k += kGsT) st[k] = start[a + k].x;
     for (unsigned k = threadIdx.x; k < len; k += kGsT) ring[k] = 0xffffu;
+    if (kSP)
+        for (unsigned k = threadIdx.x; k < len; k += kGsT) spos[k] = __ldcg(pos4 + a + k);
     for (unsigned k = threadIdx.x; 2 * k < len; k += kGsT) {
         const unsigned lo = cnt_local[a + 2 * k], hi = 2 * k + 1 < len ? cnt_local[a + 2 * k + 1] : 0u;
         cnt[k] = lo | (hi << 16);
@@ -798,16 +808,20 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
                                                                   : (lane < m ? __ldg(nbr + base + lane) : v);
                     if (base == e0) first_id = id;
                     long long ca = 0;
-                    if (stats && base == e0) {  // diagnostics: when the ids have arrived
-                        asm volatile("" ::"r"(id));
+                    if (stats && base == e0) {  // diagnostics: when the ids have arrived (the mov waits for them)
+                        unsigned t;
+                        asm volatile("mov.b32 %0, %1;" : "=r"(t) : "r"(id));
                         ca = clock64();
-                        cyc_ids += ca - c0;
+                        cyc_ids += ca - c0 + (t & 0u);
                     }
                     // Weak loads either way: the CTA- and GPU-scope acquires above order them.
-                    const float4 q = (kFlags & kGsL1Positions) ? pos4[id] : __ldcg(pos4 + id);
+                    float4 q;
+                    if (kSP && id - a < len) q = spos[id - a];
+                    else q = (kFlags & kGsL1Positions) ? pos4[id] : __ldcg(pos4 + id);
                     if (stats && base == e0) {  // ... and their positions
-                        asm volatile("" ::"f"(q.x));
-                        cyc_pos += clock64() - ca;
+                        float t;
+                        asm volatile("mov.b32 %0, %1;" : "=f"(t) : "f"(q.x));
+                        cyc_pos += clock64() - ca + (t != t ? 1 : 0);
                     }
                     // strictly in neighbour-list order; lanes past m add +0.0f (a sum that
                     // started at +0.0f is unchanged by it)
@@ -829,10 +843,20 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
                 }
                 const float n = (float)(int)(e1 - e0);
                 if (lane == 0) {
-                    __stcg(pos4 + v, make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f));
+                    const float4 np = make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f);
+                    long long cs = 0;
+                    if (stats) {  // diagnostics: the store and its fence (the movs wait for the sums)
+                        float t0, t1, t2;
+                        asm volatile("mov.b32 %0, %3; mov.b32 %1, %4; mov.b32 %2, %5;"
+                                     : "=f"(t0), "=f"(t1), "=f"(t2) : "f"(np.x), "f"(np.y), "f"(np.z));
+                        cs = clock64() + (t0 != t0 || t1 != t1 || t2 != t2 ? 1 : 0);
+                    }
+                    if (kSP) spos[v - a] = np;
+                    __stcg(pos4 + v, np);
                     // Successors in this slab read the new position after a CTA-scope
                     // acquire; successors in higher slabs get it through the sender warp.
                     __threadfence_block();
+                    if (stats) cyc_fence += clock64() - cs;
                 }
                 const long long c1 = clock64();
                 __syncwarp();
@@ -898,6 +922,7 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
             atomicAdd(stats + 4, nproc);
             atomicAdd(stats + 5, cyc_ids);
             atomicAdd(stats + 6, cyc_pos);
+            atomicAdd(stats + 7, cyc_fence);
         }
     }
 }
@@ -983,7 +1008,9 @@ void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsig
                      unsigned short *cnt_local, int *remote, uint2 *home, cudaStream_t s) {
     k_gs_setup<<<nblk(v1 - v0, 256), 256, 0, s>>>(start, nbr, v0, v1, table, cnt_local, remote, home);
 }
-size_t gs_slab_smem(unsigned S) { return 4ull * (S + 1) + 4ull * ((S + 1) / 2) + 2ull * S + 16; }
+size_t gs_slab_smem(unsigned S, unsigned flags) {
+    return (flags & kGsSmemPos) ? gs_spos_offset(S) + 16ull * S + 16 : 4ull * (S + 1) + 4ull * ((S + 1) / 2) + 2ull * S + 16;
+}
 void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s) {
     k_to_float4<<<nblk(nv, 256), 256, 0, s>>>(v3, nv, v4);
 }
@@ -991,20 +1018,24 @@ void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s
     k_from_float4<<<nblk(nv, 256), 256, 0, s>>>(v4, nv, v3);
 }
 static const void *gs_flow_fn(int threads, unsigned flags) {
-    static const void *fn[2][4] = {
+    static const void *fn[2][8] = {
         {(const void *)k_gs_flow<512, 0>, (const void *)k_gs_flow<512, 1>, (const void *)k_gs_flow<512, 2>,
-         (const void *)k_gs_flow<512, 3>},
+         (const void *)k_gs_flow<512, 3>, (const void *)k_gs_flow<512, 8>, (const void *)k_gs_flow<512, 9>,
+         (const void *)k_gs_flow<512, 10>, (const void *)k_gs_flow<512, 11>},
         {(const void *)k_gs_flow<1024, 0>, (const void *)k_gs_flow<1024, 1>, (const void *)k_gs_flow<1024, 2>,
-         (const void *)k_gs_flow<1024, 3>}};
-    return fn[threads >= 1024 ? 1 : 0][flags & 3u];
+         (const void *)k_gs_flow<1024, 3>, (const void *)k_gs_flow<1024, 8>, (const void *)k_gs_flow<1024, 9>,
+         (const void *)k_gs_flow<1024, 10>, (const void *)k_gs_flow<1024, 11>}};
+    return fn[threads >= 1024 ? 1 : 0][(flags & 3u) | ((flags & kGsSmemPos) ? 4u : 0u)];
 }
 cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax, const unsigned *table,
                            unsigned qcap, unsigned *next_slab, const uint2 *home, int P, int threads, unsigned flags,
                            const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
                            unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
                            unsigned long long *stats, cudaStream_t s) {
-    if (smax == 0 || smax > kGsSlabMaxVerts) return cudaErrorInvalidValue;
-    size_t smem = gs_slab_smem(smax);
+    if (smax == 0 || smax > kGsSlabMaxVerts || ((flags & kGsSmemPos) && smax > kGsSmemPosMaxVerts))
+        return cudaErrorInvalidValue;
+    size_t smem = gs_slab_smem(smax, flags);
+    if (smem > (size_t)kGsSlabMaxSmem) return cudaErrorInvalidValue;
     const void *fn = gs_flow_fn(threads, flags);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
     void *args[] = {&pos,    &v0,    &nv,          &smax,  (void *)&table, &qcap,         &next_slab,
@@ -1036,11 +1067,11 @@ void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes) {
     cudaGetLastError();  // the window is a hint: a refusal leaves the results unchanged
 }
 
-int gs_slab_max_blocks(int device, unsigned S, int threads) {
-    const void *fn = gs_flow_fn(threads, 0);
+int gs_slab_max_blocks(int device, unsigned S, int threads, unsigned flags) {
+    const void *fn = gs_flow_fn(threads, flags);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
     int per_sm = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads >= 1024 ? 1024 : 512, gs_slab_smem(S));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads >= 1024 ? 1024 : 512, gs_slab_smem(S, flags));
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     return per_sm * sms;
 }

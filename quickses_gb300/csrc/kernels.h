@@ -36,7 +36,7 @@ void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsig
 inline size_t gs_table_words(unsigned qcap) { return 2ull * qcap + 2; }
 void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, const unsigned *table,
                      unsigned short *cnt_local, int *remote, uint2 *home, cudaStream_t s);
-size_t gs_slab_smem(unsigned S);
+size_t gs_slab_smem(unsigned S, unsigned flags);
 void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s);
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s);
 // One Gauss-Seidel pass over vertices [v0, nv) in the table's slabs (each at most smax
@@ -47,7 +47,7 @@ cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax,
                            const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
                            unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
                            unsigned long long *stats, cudaStream_t s);
-int gs_slab_max_blocks(int device, unsigned S, int threads);
+int gs_slab_max_blocks(int device, unsigned S, int threads, unsigned flags);
 
 // Gauss-Seidel launch shape: threads per slab CTA and the slab size aimed at (vertices);
 // the result does not depend on it, only the time does.
@@ -61,6 +61,8 @@ struct GsShape {
 constexpr unsigned kGsL1Prefetch = 1;   // prefetch a successor's neighbour list into L1, not L2
 constexpr unsigned kGsL1Positions = 2;  // neighbour positions through L1 (default: L2 only)
 constexpr unsigned kGsPersistL2 = 4;    // host side: keep the positions in persisting L2 lines
+constexpr unsigned kGsSmemPos = 8;      // the slab's own positions in shared memory (slabs <= 8192)
+constexpr unsigned kGsSmemPosMaxVerts = 8192;
 // Sets (bytes > 0) or clears the stream's L2 persistence window over [p, p + bytes); the
 // set-aside is this process's context limit, restored when the window is cleared.
 void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes);

@@ -157,7 +157,9 @@ int gs_shape_candidates(GsShape *out, int max) {
     // the persisting-L2 window (kGsPersistL2) is left to callers that force it: it changes
     // stream attributes (its segment then runs outside CUDA graphs) and its reset after the
     // pass costs more than the pass gains
-    static const unsigned flags[] = {0, kGsL1Positions, kGsL1Prefetch, kGsL1Prefetch | kGsL1Positions};
+    static const unsigned flags[] = {0,          kGsL1Positions,          kGsL1Prefetch,          kGsL1Prefetch | kGsL1Positions,
+                                     kGsSmemPos, kGsSmemPos | kGsL1Positions, kGsSmemPos | kGsL1Prefetch,
+                                     kGsSmemPos | kGsL1Prefetch | kGsL1Positions};
     int k = 0;
     for (int t : {512, 1024})
         for (unsigned tg : targets)
@@ -171,6 +173,7 @@ int gs_shape_candidates(GsShape *out, int max) {
 int Arena::reserve(size_t bytes) {
     off = 0;
     if (bytes <= cap) return QSES_OK;
+    gen++;
     if (base) cudaFree(base);
     base = nullptr;
     cap = 0;
@@ -192,6 +195,7 @@ void *Arena::take(size_t bytes) {
 }
 
 void Arena::release() {
+    gen++;
     if (base) cudaFree(base);
     base = nullptr;
     cap = off = 0;
@@ -220,8 +224,9 @@ int gs_plan(int device, const GsShape &sh, unsigned nv, const unsigned *mol_off,
     // resident slab CTAs: one molecule's slabs may hold up to the largest slab; a batch's at
     // most the target, so smaller targets fit more CTAs per SM
     const bool single = mol_off == nullptr || nm <= 1;
-    const unsigned smax = single ? kGsSlabMaxVerts : std::min(std::max(sh.target, 256u), kGsSlabMaxVerts);
-    const int pmax = std::min(gs_slab_max_blocks(device, smax, sh.threads), 1024);
+    const unsigned cap = (sh.flags & kGsSmemPos) ? kGsSmemPosMaxVerts : kGsSlabMaxVerts;
+    const unsigned smax = single && !(sh.flags & kGsSmemPos) ? cap : std::min(std::max(sh.target, 256u), cap);
+    const int pmax = std::min(gs_slab_max_blocks(device, smax, sh.threads, sh.flags), 1024);
     if (pmax < 1) return QSES_ERR_NO_DEVICE;
     return gs_plan_for(pmax, sh, nv, mol_off, mol_depth, nm, pl);
 }
@@ -230,7 +235,10 @@ int gs_plan_for(int pmax, const GsShape &sh, unsigned nv, const unsigned *mol_of
                 GsPlan &pl) {
     pl = GsPlan();
     if (pmax < 1 || nv == 0) return QSES_ERR_INVALID_ARG;
-    const unsigned Smax = kGsSlabMaxVerts;
+    // with the slab's positions in shared memory (kGsSmemPos) slabs hold at most 8192
+    // vertices and a molecule may have more slabs than there are resident CTAs
+    const bool spos = (sh.flags & kGsSmemPos) != 0;
+    const unsigned Smax = spos ? kGsSmemPosMaxVerts : kGsSlabMaxVerts;
     const unsigned t = std::min(std::max(sh.target, 256u), Smax);
     const bool single = mol_off == nullptr || nm <= 1;
     const unsigned cap = sh.wave ? std::max(sh.wave, 1u) : nv;
@@ -240,6 +248,7 @@ int gs_plan_for(int pmax, const GsShape &sh, unsigned nv, const unsigned *mol_of
     // slabs of one molecule of len vertices: spread over at most pmax CTAs, at least t per slab,
     // at most Smax per slab
     auto pieces = [&](unsigned len) {
+        if (spos) return ceil_div(len, t);
         return std::max(ceil_div(len, Smax), std::min(ceil_div(len, t), (unsigned)pmax));
     };
     if (single) {
@@ -330,13 +339,17 @@ int gs_buffers(qses_context *ctx, const GsPlan &pl, unsigned nv, GsBuffers &out)
     const size_t words = pl.table.size();
     const size_t need = align256(8ull * nv + 8) + align256(4 * words) + align256(4ull * (L.wsize + L.smax + 64)) +
                         align256(4ull * (L.qcap + 2)) + 4096;
+    const void *old_ws = ctx->gs_ws.base;
     if (ctx->gs_ws.reserve(need) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "smoothing workspace");
+    if (ctx->gs_ws.base != old_ws) QSES_SEG_TRACE("smoothing workspace moved (%zu bytes)\n", need);
     out.home = (uint2 *)ctx->gs_ws.take(8ull * nv + 8);
     out.table = (unsigned *)ctx->gs_ws.take(4 * words);
     out.inbox = (unsigned *)ctx->gs_ws.take(4ull * (L.wsize + L.smax + 64));
     out.inbox_tail = (unsigned *)ctx->gs_ws.take(4ull * (L.qcap + 2));  // per slab, then the slab counter
     if (!out.inbox_tail) return ctx->fail(QSES_ERR_INTERNAL, "smoothing workspace layout");
     if (4 * words > ctx->h_gs_cap) {
+        QSES_SEG_TRACE("slab tables: pinned buffer grows to %zu words\n", words);
+        ctx->host_gen++;
         if (ctx->h_gs) cudaFreeHost(ctx->h_gs);
         ctx->h_gs = nullptr;
         ctx->h_gs_cap = 0;
@@ -384,6 +397,7 @@ int run_smoothing(qses_context *ctx, const GsShape &sh, const GsLaunch &L, int p
 
 // ---- segment 1: atoms sorted into cells, SES field codes, marching-cubes row counts
 struct FieldSeg {
+    unsigned long long mem;  // free counters of the buffers it uses
     const float *xyz, *r;
     unsigned *key, *key2, *idx, *idx2;
     float4 *atoms;
@@ -430,6 +444,7 @@ static int enqueue_field(qses_context *ctx, const FieldSeg &a, SegOut &o) {
 
 // ---- segment 2: triangles and pre-weld vertex keys, weld (sort, unique, rank, remap)
 struct MeshSeg {
+    unsigned long long mem;  // free counters of the buffers it uses
     const unsigned *sign_mask;
     const unsigned char *codes;
     const float *lut;
@@ -474,6 +489,7 @@ static int enqueue_mesh(qses_context *ctx, const MeshSeg &b, SegOut &o) {
 // ---- segment 3: closest atom, degenerate filter and host downloads on the side stream;
 // neighbour lists and Gauss-Seidel on the main stream; final read-backs
 struct FinishSeg {
+    unsigned long long mem;  // free counters of the buffers it uses
     const float4 *atoms;
     const uint2 *cells;
     const unsigned *sidx;
@@ -570,6 +586,7 @@ static int enqueue_finish(qses_context *ctx, const FinishSeg &c, SegOut &o) {
 
 int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n) {
     cudaStream_t s = ctx->stream;
+    QSES_SEG_TRACE("molecule: %u atoms, voxel %.3f, %d passes\n", n, p.voxel, p.smooth_passes);
     memset(ctx->timeline, 0, sizeof(ctx->timeline));
     ctx->tick(-1);
     ctx->launches = 0;
@@ -621,6 +638,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     Arena &A = ctx->field;
     FieldSeg a;
     memset(&a, 0, sizeof(a));
+    a.mem = ctx->input.gen + ctx->field.gen;
     a.xyz = d_xyz;
     a.r = d_r;
     a.key = (unsigned *)A.take(4ull * n);
@@ -700,6 +718,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     // ---- triangles + pre-weld vertex keys; weld
     MeshSeg b;
     memset(&b, 0, sizeof(b));
+    b.mem = ctx->field.gen + ctx->mesh_ws.gen;
     b.sign_mask = a.sign_mask;
     b.codes = a.codes;
     b.lut = a.lut;
@@ -802,6 +821,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         ctx->diag[1] = plan.max_len;
     }
     c.g = g;
+    c.mem = ctx->field.gen + ctx->mesh_ws.gen + ctx->gs_ws.gen + ctx->host_gen + pinned_frees();
     SegOut oc;
     ctx->tick(4);
     // an L2 persistence window is a stream attribute, set when the launch is enqueued
@@ -809,7 +829,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     QCHK(cudaStreamSynchronize(s));
     ctx->tick(5);
     ctx->mark("download");
-    memcpy(ctx->diag + 2, ctx->h_small + 2048, 7 * sizeof(unsigned long long));
+    memcpy(ctx->diag + 2, ctx->h_small + 2048, 8 * sizeof(unsigned long long));
     unsigned nkept = T;
     if (!keep_all && T > 0) {
         memcpy(&tot, ctx->h_small, sizeof(tot));
@@ -852,6 +872,10 @@ int qses_context::fail(int code, const char *what, cudaError_t e) {
         snprintf(buf, sizeof(buf), "%s: %s", qses_status_string(code), what);
     last_error = buf;
     return code;
+}
+
+unsigned long long qses_context::memory_generation() const {
+    return input.gen + field.gen + mesh_ws.gen + gs_ws.gen + host_gen + qses::pinned_frees();
 }
 
 void qses_context::tick(int k) {

@@ -46,6 +46,7 @@ static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 // Pinned host staging that grows geometrically and stays with the context.
 static int stage_reserve(qses_context *ctx, size_t bytes) {
     if (bytes <= ctx->h_stage_cap) return QSES_OK;
+    ctx->host_gen++;
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     ctx->h_stage = nullptr;
     ctx->h_stage_cap = 0;
@@ -61,6 +62,7 @@ static int stage_reserve(qses_context *ctx, size_t bytes) {
 
 // ---- segment 1: descriptors and atoms up, atoms sorted into cells, field, row counts
 struct BatchFieldSeg {
+    unsigned long long mem;  // free counters of the buffers it uses
     const char *h_desc;  // pinned staging; the copy nodes read it when the segment runs
     char *d_desc;
     const float *h_x;
@@ -119,6 +121,7 @@ static int enqueue_batch_field(qses_context *ctx, const BatchFieldSeg &a, SegOut
 
 // ---- segment 2: triangles and molecule-tagged weld keys, one weld for all molecules
 struct BatchMeshSeg {
+    unsigned long long mem;  // free counters of the buffers it uses
     const unsigned *sign_mask;
     const unsigned char *codes;
     const uint2 *rows;
@@ -173,6 +176,7 @@ static int enqueue_batch_mesh(qses_context *ctx, const BatchMeshSeg &m, SegOut &
 // ---- segment 3: closest atom, per-molecule filter and host downloads on the side stream;
 // neighbour lists and one Gauss-Seidel dataflow over all molecules on the main stream
 struct BatchFinishSeg {
+    unsigned long long mem;  // free counters of the buffers it uses
     const float4 *atoms;
     const uint2 *cells;
     const unsigned *sidx, *vmol;
@@ -274,6 +278,7 @@ static int enqueue_batch_finish(qses_context *ctx, const BatchFinishSeg &c, SegO
 
 int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int passes, int key_bits) {
     cudaStream_t s = ctx->stream;
+    QSES_SEG_TRACE("batch: %u molecules, %d passes\n", count, passes);
     memset(ctx->timeline, 0, sizeof(ctx->timeline));
     ctx->tick(-1);
     ctx->launches = 0;
@@ -366,6 +371,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     Arena &A = ctx->field;
     BatchFieldSeg a;
     memset(&a, 0, sizeof(a));
+    a.mem = ctx->field.gen + ctx->host_gen;
     a.h_desc = hs;
     a.d_desc = (char *)A.take(desc_bytes);
     a.h_x = hx;
@@ -469,6 +475,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     // ---- triangles + molecule-tagged weld keys, then one weld for all molecules
     BatchMeshSeg mb;
     memset(&mb, 0, sizeof(mb));
+    mb.mem = ctx->field.gen + ctx->mesh_ws.gen + ctx->host_gen;
     mb.sign_mask = a.sign_mask;
     mb.codes = a.codes;
     mb.rows = a.rows;
@@ -578,6 +585,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         ctx->diag[1] = std::max<unsigned long long>(ctx->diag[1], plan.max_len);
     }
     c.b = b;
+    c.mem = ctx->field.gen + ctx->mesh_ws.gen + ctx->gs_ws.gen + ctx->host_gen + pinned_frees();
     SegOut oc;
     ctx->tick(4);
     // an L2 persistence window is a stream attribute, set when the launch is enqueued

@@ -16,6 +16,7 @@ namespace qses {
 struct Arena {
     void *base = nullptr;
     size_t cap = 0, off = 0;
+    unsigned long long gen = 0;  // bumped whenever the allocation is freed (or replaced)
     int reserve(size_t bytes);  // resets the bump pointer; grows (and invalidates) if needed
     void *take(size_t bytes);   // 256-byte aligned; null when out of room
     void release();
@@ -61,6 +62,8 @@ namespace qses {
 // Pinned host blocks from the process-wide cache (released blocks are reused).
 void *pinned_take(size_t bytes, size_t *got);
 void pinned_give(void *p, size_t bytes);
+// Count of pinned blocks the cache has freed so far (any context's).
+unsigned long long pinned_frees();
 
 // Host destination of a qses_compute call, filled by the pipeline while the smoothing pass
 // still runs: [vertices 12 nv | triangles 12 T (upper bound) | atom_sorted 4 nv | atom_input 4 nv].
@@ -100,6 +103,7 @@ struct GraphSeg {
     std::vector<unsigned char> key;
     SegOut out;
     unsigned long long used = 0;
+    unsigned long long mem = 0;  // the context's memory generation when it was captured
 };
 // Graphs kept per segment slot (a batch call split by smoothing passes alternates shapes).
 constexpr int kSegCache = 4;
@@ -141,6 +145,11 @@ struct qses_context {
     bool use_graphs = true;           // pipeline segments through CUDA graphs
     qses::GraphSeg seg[qses::kSegSlots][qses::kSegCache];
     unsigned long long seg_clock = 0;
+    // Free counters of the buffers graphs may use (see segment.h): arenas count their own;
+    // host_gen counts pinned staging and slab-table reallocations; pinned_frees() the
+    // process-wide pinned block cache.
+    unsigned long long host_gen = 0;
+    unsigned long long memory_generation() const;  // the sum of them all
     unsigned long long graph_stats[4] = {0};  // captures, instantiations, in-place updates, replays
     // host timeline of the last pipeline call (ms): host work before the first launch, field
     // segment (launch to read-back), host gap, mesh segment, host gap, finish segment

@@ -13,6 +13,10 @@
 //     entry, or, with the slot's entries all taken, the least recently used executable is
 //     updated in place (cudaGraphExecUpdate: same topology, new parameters), or
 //     re-instantiated when the topology differs.
+// Copy and memset nodes stay bound to the allocations they were captured with, even when a
+// freed buffer comes back at the same address.  So every key also holds the sum of the
+// free counters of the buffers its segment uses (the counters only grow), and an entry
+// captured before any buffer of the context was freed is destroyed rather than updated.
 // Capture runs on a private stream of the context (nothing another thread enqueues can fall
 // into it, and a caller's stream is never put in capture mode); the graph is then launched on
 // the context's stream.  Work on the side stream joins the capture through the fork event
@@ -20,6 +24,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 
@@ -29,6 +35,19 @@ namespace qses {
 
 template <class K>
 using SegFn = int (*)(qses_context *, const K &, SegOut &);
+
+// QSES_TRACE=1 in the environment: one stderr line per graph action (for locating failures).
+inline bool seg_trace() {
+    static const bool on = getenv("QSES_TRACE") != nullptr;
+    return on;
+}
+#define QSES_SEG_TRACE(...)                       \
+    do {                                          \
+        if (seg_trace()) {                        \
+            fprintf(stderr, "[qses] " __VA_ARGS__); \
+            fflush(stderr);                       \
+        }                                         \
+    } while (0)
 
 // Ends a capture that the enqueue function left early on an error.
 inline void abandon_capture(qses_context *ctx) {
@@ -64,6 +83,7 @@ int run_segment(qses_context *ctx, int slot, const K &key, SegOut &out, SegFn<K>
         out.launches = ctx->launches - l0;
         return rc;
     }
+    const unsigned long long mem = ctx->memory_generation();
     GraphSeg *cache = ctx->seg[slot];
     cudaStream_t s = ctx->stream;
     cudaError_t e;
@@ -71,6 +91,7 @@ int run_segment(qses_context *ctx, int slot, const K &key, SegOut &out, SegFn<K>
     for (int i = 0; i < kSegCache; i++) {
         GraphSeg &c = cache[i];
         if (c.exec && c.key.size() == sizeof(K) && memcmp(c.key.data(), &key, sizeof(K)) == 0) {
+            QSES_SEG_TRACE("slot %d replay entry %d\n", slot, i);
             e = cudaGraphLaunch(c.exec, s);
             if (e != cudaSuccess) return ctx->fail(QSES_ERR_CUDA, "graph launch", e);
             c.used = now;
@@ -91,6 +112,7 @@ int run_segment(qses_context *ctx, int slot, const K &key, SegOut &out, SegFn<K>
     }
     GraphSeg &gs = cache[victim];
     gs.key.clear();
+    QSES_SEG_TRACE("slot %d capture into entry %d (%s)\n", slot, victim, gs.exec ? "occupied" : "free");
     cudaGraph_t g = nullptr;
     {
         CaptureStream cs(ctx);
@@ -109,8 +131,14 @@ int run_segment(qses_context *ctx, int slot, const K &key, SegOut &out, SegFn<K>
         return ctx->fail(QSES_ERR_CUDA, "graph capture", e);
     }
     ctx->graph_stats[0]++;
+    if (gs.exec && gs.mem != mem) {  // it may use freed buffers: never update it, start afresh
+        QSES_SEG_TRACE("slot %d entry %d predates a freed buffer: dropped\n", slot, victim);
+        cudaGraphExecDestroy(gs.exec);
+        gs.exec = nullptr;
+    }
     if (gs.exec) {
         cudaGraphExecUpdateResultInfo info;
+        QSES_SEG_TRACE("slot %d update entry %d\n", slot, victim);
         if (cudaGraphExecUpdate(gs.exec, g, &info) == cudaSuccess) {
             ctx->graph_stats[2]++;
         } else {
@@ -120,6 +148,7 @@ int run_segment(qses_context *ctx, int slot, const K &key, SegOut &out, SegFn<K>
         }
     }
     if (!gs.exec) {
+        QSES_SEG_TRACE("slot %d instantiate entry %d\n", slot, victim);
         e = cudaGraphInstantiate(&gs.exec, g, 0);
         if (e != cudaSuccess) {
             gs.exec = nullptr;
@@ -133,6 +162,8 @@ int run_segment(qses_context *ctx, int slot, const K &key, SegOut &out, SegFn<K>
     gs.key.assign((const unsigned char *)&key, (const unsigned char *)&key + sizeof(K));
     gs.out = out;
     gs.used = now;
+    gs.mem = mem;
+    QSES_SEG_TRACE("slot %d launch entry %d\n", slot, victim);
     e = cudaGraphLaunch(gs.exec, s);
     if (e != cudaSuccess) {
         gs.key.clear();

@@ -93,7 +93,8 @@ def test_cache_full_updates_in_place(direct):
             xyz = (base + rng.normal(0, 0.25, base.shape)).astype(np.float32)
             _same(g.compute(xyz, rad, voxel=0.5, smooth=1), direct.compute(xyz, rad, voxel=0.5, smooth=1))
         st = g.graph_stats()
-        assert st["updates"] >= 3 and st["instantiations"] <= 3 * 4
+        # (entries captured before an arena grew are instantiated afresh, never updated)
+        assert st["updates"] >= 3 and st["instantiations"] + st["updates"] == st["captures"]
 
 
 def test_forced_smoothing_shapes_and_waves(direct):
@@ -158,14 +159,15 @@ def test_batch_graphs_match_direct(direct):
     want = direct.compute_batch(reqs)
     with q.Context(0) as g:
         g.set_smoothing_shape(1024, 16384, 0, 0)
-        s0 = g.graph_stats()
-        for rep in range(3):
+        for rep in range(4):
+            if rep == 2:  # workspaces have their final sizes after two calls
+                s0 = g.graph_stats()
             got = g.compute_batch(reqs)
             for a, b in zip(got, want):
                 _same(a, b)
         d = _delta(g.graph_stats(), s0)
         # two batches per call (1 and 2 smoothing passes), each with its cached graphs
-        assert d["captures"] == 6 and d["replays"] == 12
+        assert d["captures"] == 0 and d["replays"] == 12
         # trajectory-like: the same molecules moved
         rng = np.random.default_rng(9)
         moved = [dict(r, xyz=(r["xyz"] + rng.normal(0, 0.2, r["xyz"].shape)).astype(np.float32)) for r in reqs]

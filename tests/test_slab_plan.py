@@ -17,31 +17,33 @@ from quickses_gb300 import _lib as L
 SMAX = 25000
 
 
-def _plan(nv, mol_off=None, depth=None, threads=1024, target=16384, wave=0, pmax=152):
+def _plan(nv, mol_off=None, depth=None, threads=1024, target=16384, wave=0, pmax=152, flags=0):
     lib = L.lib()
     launch = (ctypes.c_uint * 6)()
     nm = 1 if mol_off is None else len(mol_off) - 1
     mo = None if mol_off is None else np.ascontiguousarray(mol_off, np.uint32)
     dp = None if depth is None else np.ascontiguousarray(depth, np.int32)
     rc = lib.qses_debug_slab_plan(nv, None if mo is None else mo.ctypes.data, None if dp is None else dp.ctypes.data,
-                                  nm, threads, target, wave, pmax, launch, None, 0)
+                                  nm, threads, target, flags, wave, pmax, launch, None, 0)
     assert rc == 0, rc
     ctas, smax, qcap, wsize, waves, words = list(launch)
     table = np.zeros(waves * words, np.uint32)
     rc = lib.qses_debug_slab_plan(nv, None if mo is None else mo.ctypes.data, None if dp is None else dp.ctypes.data,
-                                  nm, threads, target, wave, pmax, launch, table.ctypes.data, table.size)
+                                  nm, threads, target, flags, wave, pmax, launch, table.ctypes.data, table.size)
     assert rc == 0
     out = []
     for w in range(waves):
         t = table[w * words:(w + 1) * words]
         Q = int(t[0])
         out.append((np.array(t[1:Q + 2], np.int64), np.array(t[qcap + 2:qcap + 2 + Q], np.int64)))
-    return dict(ctas=ctas, smax=smax, qcap=qcap, wsize=wsize, waves=waves, target=target), out
+    return dict(ctas=ctas, smax=smax, qcap=qcap, wsize=wsize, waves=waves, target=target, flags=flags), out
 
 
 def _check(nv, mol_off, info, waves, pmax=152):
     mol_off = np.array([0, nv] if mol_off is None else mol_off, np.int64)
     assert info["ctas"] == min(pmax, info["qcap"]) and info["smax"] <= SMAX
+    if info["flags"] & 8:  # slab positions in shared memory: at most 8192 vertices per slab
+        assert info["smax"] <= max(256, min(info["target"], 8192))
     if mol_off is not None and len(mol_off) > 2:
         assert info["smax"] <= max(256, min(info["target"], SMAX))
     v0 = 0
@@ -112,5 +114,29 @@ def test_order_follows_expected_start():
 def test_invalid():
     lib = L.lib()
     launch = (ctypes.c_uint * 6)()
-    assert lib.qses_debug_slab_plan(0, None, None, 1, 1024, 4096, 0, 152, launch, None, 0) != 0
-    assert lib.qses_debug_slab_plan(10, None, None, 1, 1024, 4096, 0, 0, launch, None, 0) != 0
+    assert lib.qses_debug_slab_plan(0, None, None, 1, 1024, 4096, 0, 0, 152, launch, None, 0) != 0
+    assert lib.qses_debug_slab_plan(10, None, None, 1, 1024, 4096, 0, 0, 0, launch, None, 0) != 0
+
+
+@pytest.mark.parametrize("nv,target", [(1, 4096), (29938, 4096), (3540690, 8192), (3540690, 20000),
+                                       (17_000_000, 4096)])
+def test_shared_memory_positions_split(nv, target):
+    # one molecule, slab positions in shared memory: slabs of at most min(target, 8192),
+    # as many as needed (more than the resident CTAs), taken in id order
+    info, waves = _plan(nv, target=target, flags=8)
+    _check(nv, None, info, waves)
+    bnd, order = waves[0]
+    S = -(-nv // -(-nv // min(target, 8192)))
+    assert np.array_equal(bnd[:-1], np.arange(0, nv, S)) and np.array_equal(order, np.arange(len(order)))
+    assert info["smax"] <= 8192
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_batches_shared_memory_positions(seed):
+    rng = np.random.default_rng(100 + seed)
+    nm = int(rng.integers(2, 200))
+    sizes = np.exp(rng.uniform(np.log(1), np.log(1_000_000), nm)).astype(np.int64)
+    mol_off = np.concatenate([[0], np.cumsum(sizes)])
+    nv = int(mol_off[-1])
+    info, waves = _plan(nv, mol_off, rng.integers(20, 700, nm), target=25000, flags=11)
+    _check(nv, mol_off, info, waves)
