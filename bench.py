@@ -63,6 +63,12 @@ class ClockSampler:
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+            # nvidia-smi's start-up (driver queries) slows CUDA calls made meanwhile: the timed
+            # region starts once the first sample is written (sampling continues through it)
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 3.0 and os.path.getsize(self.path) == 0:
+                time.sleep(0.02)
+            time.sleep(0.1)
         except Exception:
             self.proc = None
         return self
@@ -453,7 +459,8 @@ def run_served_form(args):
     sweep = []
     with q.Context(0) as tctx:  # launch-shape tuning on a sample (process-wide, like a service start)
         tune = tctx.autotune_batch(reqs[-64:-32])
-    with q.Server(lanes=args.lanes, memory_budget=120 << 30, max_batch=256) as srv:
+    with q.Server(lanes=args.lanes, memory_budget=120 << 30, max_batch=256,
+                  max_batch_voxels=int(args.batch_voxels) if args.batch_voxels else None) as srv:
         for r in reqs[-64:]:  # warm-up: workspaces and pinned blocks grow to size once
             srv.wait(srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"]))
         with ClockSampler(0) as clk:
@@ -502,6 +509,7 @@ def run_served_form(args):
         "config": {"workload": "open-loop Poisson, %d requests per offered rate, atom counts log-uniform in "
                                "[200, 200000], voxel one of {0.3, 0.4, 0.5} A, 1 pass" % per_rate,
                    "form": "served", "lanes": args.lanes, "memory_budget_gb": 120,
+                   "max_batch_voxels": args.batch_voxels or 1e9,
                    "smoothing_shape": {"threads": tune[0], "slab_target": tune[1], "cache_flags": tune[2]}},
         "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "sweep": sweep, "server": stats,
         "plain_path": {"value": plain, "unit": "molecules/s",
@@ -525,6 +533,8 @@ def main():
     ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="served form: offered requests/s")
     ap.add_argument("--requests", type=int, default=1000, help="served form: requests per offered rate")
     ap.add_argument("--lanes", type=int, default=2, help="served form: batches in flight")
+    ap.add_argument("--batch-voxels", type=float, default=0,
+                    help="served form: grid voxels per batch (0 = the server's default)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")
     ap.add_argument("--gs-shape", default="", help="profile-once: smoothing shape threads,target,cache_flags")
     ap.add_argument("--profile-once", action="store_true",

@@ -14,9 +14,11 @@
 //                 updated once every lower-id neighbour has been, exactly as the sequential
 //                 loop would see them.
 #include <cfloat>
+#include <cstdlib>
 #include <cstring>
 
 #include "device_common.cuh"
+
 #include "kernels.h"
 #include "mc_tables.h"
 
@@ -633,7 +635,8 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 }
 
 // Persistent CTAs take the wave's slabs from a counter, in the table's order (a slab only
-// waits for slabs taken before it, by CTAs that are running, so every wait ends).  Per slab,
+// waits for slabs taken before it, by CTAs that were running when they took them, so every
+// wait ends without a co-residency guarantee).  Per slab,
 // warp 0 takes boundary arrivals from lower slabs, warp 1 sends this slab's cross-slab
 // releases (GPU-scope atomics, off the workers' critical path), the other warps update
 // vertices.  Table: Q, the Q + 1 slab bounds in id order (qcap + 1 slots), then the Q slab ids
@@ -645,7 +648,8 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
                                                   const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
                                                   const unsigned short *__restrict__ cnt_local, int *remote,
                                                   unsigned *inbox, unsigned *inbox_tail, int *err,
-                                                  long long spin_cycles, unsigned long long *stats) {
+                                                  long long spin_cycles, unsigned long long *stats,
+                                                  unsigned idle_ns_max) {
     extern __shared__ unsigned s_dyn[];
     __shared__ unsigned s_head, s_tail, s_done, s_stop, s_ob_head, s_ob_tail, s_slab;
     __shared__ unsigned s_ob[kGsOutbox];
@@ -768,7 +772,11 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
             }
         }
     } else {
-        // Worker warps: one vertex per warp; lanes fetch neighbours in parallel.
+        // Worker warps: one vertex per warp; lanes fetch neighbours in parallel.  An idle
+        // worker backs off (32 ns doubling up to idle_ns_max, 1 us by default): a hot polling loop of up to
+        // 30 warps would take issue slots and shared-memory bandwidth from the warps on the
+        // critical path.
+        unsigned idle_ns = 0;
         for (;;) {
             unsigned v = 0xffffffffu, quit = 0;
             if (lane == 0) {
@@ -790,9 +798,11 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
             quit = __shfl_sync(0xffffffffu, quit, 0);
             if (quit) break;
             if (v == 0xffffffffu) {
-                __nanosleep(20);
+                idle_ns = idle_ns ? min(2 * idle_ns, idle_ns_max) : 32u;
+                __nanosleep(idle_ns);
                 continue;
             }
+            idle_ns = 0;
             // Neighbour ids of the vertex this warp continues with, loaded as soon as the
             // release picked it (the lists are constant, so the early load is always valid).
             unsigned pre_v = 0xffffffffu, pre_id = 0u;
@@ -1038,10 +1048,20 @@ cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax,
     if (smem > (size_t)kGsSlabMaxSmem) return cudaErrorInvalidValue;
     const void *fn = gs_flow_fn(threads, flags);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
+    // longest sleep of an idle worker warp (ns); QSES_GS_IDLE_NS overrides it
+    static const unsigned idle_ns_max = [] {
+        const char *e = getenv("QSES_GS_IDLE_NS");
+        const long v = e ? strtol(e, nullptr, 10) : 0;
+        return v >= 32 && v <= 100000 ? (unsigned)v : 1024u;
+    }();
+    unsigned idle = idle_ns_max;
     void *args[] = {&pos,    &v0,    &nv,          &smax,  (void *)&table, &qcap,         &next_slab,
                     (void *)&home, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
-                    &inbox_tail, &err, &spin_cycles, &stats};
-    return cudaLaunchCooperativeKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
+                    &inbox_tail, &err, &spin_cycles, &stats, &idle};
+    // A plain launch: a CTA only waits for slabs taken before its own, by CTAs that were
+    // running when they took them, so no co-residency guarantee is needed, and other kernels
+    // (the side stream's, another lane's) may share the SMs.  P is at most what fits resident.
+    return cudaLaunchKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
 }
 void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes) {
     int max_persist = 0, max_window = 0;
