@@ -15,6 +15,8 @@ CPU field code, so this is the CPU oracle port (C++/OpenMP restatement) on the s
 workload, the whole pipeline per step.
 """
 import argparse
+import atexit
+import datetime
 import ctypes
 import json
 import os
@@ -47,34 +49,41 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+    """nvidia-smi clocks/throttle sampling.  Started before the warm-up (nvidia-smi's start-up
+    slows CUDA calls for a while), summarised over the samples stamped between mark() and
+    stop(): the timed region."""
 
     def __init__(self, device=0):
         self.proc = None
         self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
         self.device = device
+        self.t0 = self.t1 = None
 
-    def __enter__(self):
+    def start(self):
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.device), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=timestamp,clocks.sm,clocks.max.sm,power.draw,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
-            # nvidia-smi's start-up (driver queries) slows CUDA calls made meanwhile: the timed
-            # region starts once the first sample is written (sampling continues through it)
-            t0 = time.perf_counter()
-            while time.perf_counter() - t0 < 3.0 and os.path.getsize(self.path) == 0:
-                time.sleep(0.02)
-            time.sleep(0.1)
         except Exception:
             self.proc = None
+        if self.proc:
+            atexit.register(self._kill)  # never leave the sampler behind
         return self
 
-    def __exit__(self, *exc):
-        if self.proc:
+    def _kill(self):
+        if self.proc and self.proc.poll() is None:
+            self.proc.terminate()
+
+    def mark(self):
+        self.t0 = datetime.datetime.now()
+
+    def stop(self):
+        self.t1 = datetime.datetime.now()
+        if self.proc and self.proc.poll() is None:
             time.sleep(0.15)
             self.proc.terminate()
             self.proc.wait(timeout=5)
@@ -82,11 +91,19 @@ class ClockSampler:
 
     def summary(self):
         try:
-            rows = [ln.split(",") for ln in open(self.path).read().strip().splitlines()]
-            sm = [float(r[0]) for r in rows if r[0].strip().replace(".", "").isdigit()]
-            mx = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+            rows = []
+            for ln in open(self.path).read().strip().splitlines():
+                r = [x.strip() for x in ln.split(",")]
+                try:
+                    ts = datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f")
+                except ValueError:
+                    continue
+                if (self.t0 is None or ts >= self.t0) and (self.t1 is None or ts <= self.t1):
+                    rows.append(r[1:])
+            sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+            mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
             names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-            reasons = sorted({names[q] for r in rows for q in range(4) if len(r) > 3 + q and r[3 + q].strip() == "Active"})
+            reasons = sorted({names[q] for r in rows for q in range(4) if len(r) > 3 + q and r[3 + q] == "Active"})
             return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                     "reasons": reasons, "samples": len(sm)}
         except Exception as e:  # noqa: BLE001
@@ -168,6 +185,7 @@ def run_gpu(args):
     with torch.cuda.stream(stream):
         # launch-shape tuning of the smoothing kernel (same mesh for every shape), before
         # the warm-up: it runs the pipeline once per candidate shape
+        clk = ClockSampler(local).start()
         tuned = ctx.autotune(xyz, rad, voxel=wl.voxel, smooth=wl.smooth) if wl.smooth > 0 else None
         for _ in range(args.warmup):
             dm = step()
@@ -183,20 +201,21 @@ def run_gpu(args):
         if world > 1:
             dist.barrier()
         times = []
-        with ClockSampler(local) as clk:
-            torch.cuda.synchronize()
-            t_wall0 = time.perf_counter()
-            for _ in range(args.steps):
-                flush.zero_()  # L2 flush between steps, outside the event pair
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                dm = step()
-                e1.record(stream)
-                e1.synchronize()
-                times.append(e0.elapsed_time(e1))
-            torch.cuda.synchronize()
-            t_wall = time.perf_counter() - t_wall0
+        torch.cuda.synchronize()
+        clk.mark()
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between steps, outside the event pair
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dm = step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+        clk.stop()
         ms = float(np.mean(times))
         graphs_timed = ctx.graph_stats()
     nv, nt = dm.n_vertices, dm.n_triangles
@@ -402,6 +421,7 @@ def run_batch_form(args):
     arrays, rr = A._requests(reqs)
     with q.Context(0) as ctx:
         ctx.set_graphs(not args.no_graphs)
+        clk = ClockSampler(0).start()
         tune = ctx.autotune_batch(reqs)  # launch-shape tuning, before the warm-up
         for _ in range(args.warmup):
             _raw_batch(lib, L, ctx, rr, n)
@@ -411,11 +431,12 @@ def run_batch_form(args):
         launches = ctx.last_launch_count()
         ctx.set_profiling(False)
         times = []
-        with ClockSampler(0) as clk:
-            for _ in range(args.steps):
-                t0 = time.perf_counter()
-                nv, nt, bad = _raw_batch(lib, L, ctx, rr, n)
-                times.append(time.perf_counter() - t0)
+        clk.mark()
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            nv, nt, bad = _raw_batch(lib, L, ctx, rr, n)
+            times.append(time.perf_counter() - t0)
+        clk.stop()
         sec = float(np.mean(times))
         graphs_timed = ctx.graph_stats()
         timeline = ctx.host_timeline()
@@ -457,41 +478,43 @@ def run_served_form(args):
     reqs = q.molecules.served_stream(per_rate * len(rates) + 64)
     rng = np.random.default_rng(11)
     sweep = []
+    clk = ClockSampler(0).start()
     with q.Context(0) as tctx:  # launch-shape tuning on a sample (process-wide, like a service start)
         tune = tctx.autotune_batch(reqs[-64:-32])
     with q.Server(lanes=args.lanes, memory_budget=120 << 30, max_batch=256,
                   max_batch_voxels=int(args.batch_voxels) if args.batch_voxels else None) as srv:
         for r in reqs[-64:]:  # warm-up: workspaces and pinned blocks grow to size once
             srv.wait(srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"]))
-        with ClockSampler(0) as clk:
-            for ri, rate in enumerate(rates):
-                chunk = reqs[ri * per_rate:(ri + 1) * per_rate]
-                arrivals = np.cumsum(rng.exponential(1.0 / rate, per_rate))
-                tickets = [None] * per_rate
+        clk.mark()
+        for ri, rate in enumerate(rates):
+            chunk = reqs[ri * per_rate:(ri + 1) * per_rate]
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, per_rate))
+            tickets = [None] * per_rate
 
-                def submitter():
-                    t0 = time.perf_counter()
-                    for k, r in enumerate(chunk):
-                        d = t0 + arrivals[k] - time.perf_counter()
-                        if d > 0:
-                            time.sleep(d)
-                        tickets[k] = srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"])
+            def submitter():
+                t0 = time.perf_counter()
+                for k, r in enumerate(chunk):
+                    d = t0 + arrivals[k] - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    tickets[k] = srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"])
 
-                t_start = time.perf_counter()
-                th = threading.Thread(target=submitter)
-                th.start()
-                lat = []
-                for k in range(per_rate):
-                    while tickets[k] is None:
-                        time.sleep(0.0002)
-                    _, info = srv.wait(tickets[k])
-                    lat.append(info["total_s"])
-                t_end = time.perf_counter()
-                th.join()
-                lat = np.array(lat) * 1e3
-                sweep.append({"offered_per_s": rate, "achieved_per_s": per_rate / (t_end - t_start),
-                              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                              "requests": per_rate})
+            t_start = time.perf_counter()
+            th = threading.Thread(target=submitter)
+            th.start()
+            lat = []
+            for k in range(per_rate):
+                while tickets[k] is None:
+                    time.sleep(0.0002)
+                _, info = srv.wait(tickets[k])
+                lat.append(info["total_s"])
+            t_end = time.perf_counter()
+            th.join()
+            lat = np.array(lat) * 1e3
+            sweep.append({"offered_per_s": rate, "achieved_per_s": per_rate / (t_end - t_start),
+                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                          "requests": per_rate})
+        clk.stop()
         stats = srv.stats()
     # the plain per-request path on the same GPU: one qses_compute at a time, closed loop
     from quickses_gb300 import _lib as L
