@@ -271,7 +271,7 @@ def run_gpu(args):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "smoothing_shape": None if tuned is None else
                    {"threads": tuned[0], "slab_target": tuned[1], "cache_flags": tuned[2]},
-                   "refine_tile": None if tuned is None else ("16x8" if tuned[3] == 1 else "8x8"),
+                   "refine_tile": None if tuned is None else ["8x8", "16x8", "16x16", "32x16"][tuned[3]],
                    "cuda_graphs": _graph_summary(args, graphs_timed)},
         "e2e": {"value": e2e_value, "unit": "voxels/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

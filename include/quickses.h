@@ -172,8 +172,9 @@ QSES_API void qses_set_pinned_cache(unsigned long long bytes);
 QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_float3 *atoms, const float *radii,
                            unsigned n, int repeats, int *threads_out, unsigned *target_out, unsigned *flags_out,
                            int *field_shape_out, float *smooth_ms_out);
-/* Fixes the refine tile shape of ctx: 0 = 8 x 8 z-rows per CTA, 1 = 16 x 8 (less halo per
- * row, more shared memory); -1 returns to the tuned/default shape.  Same codes for both. */
+/* Fixes the refine tile shape of ctx: 0 = 8 x 8 z-rows per CTA, 1 = 16 x 8, 2 = 16 x 16,
+ * 3 = 32 x 16 (less halo per row, more shared memory); -1 returns to the tuned/default
+ * shape.  Same codes for all. */
 QSES_API int qses_set_field_shape(qses_context *ctx, int shape);
 /* Fixes the smoothing launch shape of ctx: threads 512 or 1024 per slab CTA, slab size
  * aimed at (>= 256 vertices), cache_flags bit 0 = prefetch successors' neighbour lists into

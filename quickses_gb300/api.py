@@ -174,7 +174,7 @@ class Context:
         return th.value, tg.value, fl.value, fs.value, ms.value
 
     def set_field_shape(self, shape=-1):
-        """Fix the refine tile shape (0: 8 x 8 rows, 1: 16 x 8); -1 = tuned/default."""
+        """Fix the refine tile shape (0: 8 x 8 rows, 1: 16 x 8, 2: 16 x 16, 3: 32 x 16); -1 = tuned/default."""
         self._check(self._lib.qses_set_field_shape(self._h, int(shape)), "qses_set_field_shape")
 
     def autotune_batch(self, requests, repeats=1):

@@ -227,19 +227,35 @@ constexpr int kEdtNT = 256;
 
 // One refine tile: z-word w of the TX x TY rows starting at (TX ib, TY jb), with an R halo.
 // Larger tiles re-read less halo per row (the z pass runs on (TX+2R)(TY+2R) rows for TX TY
-// output rows) at the cost of shared memory; the shape is chosen by the autotuner.
+// output rows) at the cost of shared memory (dynamic, edt_smem_bytes); the shape is chosen
+// by the autotuner.
+
+template <int TX, int TY>
+struct EdtSmem {
+    static constexpr int HXM = TX + 2 * QSES_RMAX, HYM = TY + 2 * QSES_RMAX;
+    static constexpr size_t out_off = 0;                                          // [HXM HYM][3] words
+    static constexpr size_t g_off = (out_off + 12ull * HXM * HYM + 15) & ~15ull;  // [HXM HYM][32] bytes
+    static constexpr size_t h_off = g_off + 32ull * HXM * HYM;                    // [HXM][TY][32] bytes
+    static constexpr size_t in_off = h_off + 32ull * HXM * TY;                    // [TX TY] words
+    static constexpr size_t ot_off = in_off + 4ull * TX * TY;                     // [TX TY] words
+    static constexpr size_t bytes = ot_off + 4ull * TX * TY;
+};
 
 template <int TX, int TY>
 __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, const unsigned *__restrict__ inMask,
                                          const unsigned *__restrict__ outMask, unsigned char *__restrict__ codes,
                                          unsigned *__restrict__ signMask) {
-    constexpr int HXM = TX + 2 * QSES_RMAX, HYM = TY + 2 * QSES_RMAX;
-    __shared__ unsigned s_out[HXM * HYM][3];
+    using L = EdtSmem<TX, TY>;
+    constexpr int HYM = L::HYM;
+    extern __shared__ __align__(16) unsigned char edt_smem[];
+    unsigned (*s_out)[3] = reinterpret_cast<unsigned (*)[3]>(edt_smem + L::out_off);
     // Squared distances, one byte per voxel (255 = none); the y and x passes work on four
     // voxels per 32-bit word with saturating byte adds, so 255 stays "none".
-    __shared__ __align__(16) unsigned char s_g[HXM * HYM][32];
-    __shared__ __align__(16) unsigned char s_h[HXM][TY][32];
-    __shared__ unsigned s_in[TX * TY], s_ot[TX * TY];
+    unsigned char (*s_g)[32] = reinterpret_cast<unsigned char (*)[32]>(edt_smem + L::g_off);
+    unsigned char (*s_h)[TY][32] = reinterpret_cast<unsigned char (*)[TY][32]>(edt_smem + L::h_off);
+    unsigned *s_in = reinterpret_cast<unsigned *>(edt_smem + L::in_off);
+    unsigned *s_ot = reinterpret_cast<unsigned *>(edt_smem + L::ot_off);
+    (void)HYM;
     const int j0 = jb * TY, i0 = ib * TX;
     const int R = g.R, G = g.G, W = g.W, t = threadIdx.x;
     const int HX = TX + 2 * R, HY = TY + 2 * R, k0 = w * 32;
@@ -417,19 +433,35 @@ void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigne
     dim3 grid(g.W, (g.G + kSasTY - 1) / kSasTY, (g.G + kSasTX - 1) / kSasTX);
     k_sas<<<grid, kSasNT, 0, s>>>(g, atoms, cells, inMask, outMask);
 }
+template <int TX, int TY>
+static void launch_edt_shape(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
+                             unsigned *signMask, cudaStream_t s) {
+    constexpr size_t smem = EdtSmem<TX, TY>::bytes;
+    static const bool attr = [] {
+        return cudaFuncSetAttribute((const void *)k_edt<TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem) == cudaSuccess;
+    }();
+    (void)attr;
+    dim3 grid(g.W, (g.G + TY - 1) / TY, (g.G + TX - 1) / TX);
+    k_edt<TX, TY><<<grid, kEdtNT, smem, s>>>(g, inMask, outMask, codes, signMask);
+}
+
 void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
                 unsigned *signMask, cudaStream_t s, int shape) {
-    // shape 0: 8 x 8 rows (37 KB of shared memory), 1: 16 x 8 rows (48 KB, the static limit)
-    const int TX = shape >= 1 ? 16 : 8, TY = 8;
-    dim3 grid(g.W, (g.G + TY - 1) / TY, (g.G + TX - 1) / TX);
-    if (shape >= 1) k_edt<16, 8><<<grid, kEdtNT, 0, s>>>(g, inMask, outMask, codes, signMask);
-    else k_edt<8, 8><<<grid, kEdtNT, 0, s>>>(g, inMask, outMask, codes, signMask);
+    // shape 0: 8 x 8 rows (37 KB of shared memory), 1: 16 x 8 (48 KB), 2: 16 x 16 (66 KB),
+    // 3: 32 x 16 (99 KB)
+    switch (shape) {
+        case 3: launch_edt_shape<32, 16>(g, inMask, outMask, codes, signMask, s); break;
+        case 2: launch_edt_shape<16, 16>(g, inMask, outMask, codes, signMask, s); break;
+        case 1: launch_edt_shape<16, 8>(g, inMask, outMask, codes, signMask, s); break;
+        default: launch_edt_shape<8, 8>(g, inMask, outMask, codes, signMask, s); break;
+    }
 }
-static unsigned persistent_blocks(const void *fn, int threads, unsigned items) {
+static unsigned persistent_blocks(const void *fn, int threads, unsigned items, size_t smem = 0) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
     unsigned blocks = (unsigned)(sms * (per_sm > 0 ? per_sm : 1));
     return items < blocks ? (items ? items : 1u) : blocks;
 }
@@ -440,7 +472,8 @@ void launch_sas_batch(const QBatch &b, unsigned tiles, const float4 *atoms, cons
 }
 void launch_edt_batch(const QBatch &b, unsigned tiles, const unsigned *inMask, const unsigned *outMask,
                       unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s) {
-    k_edt_batch<<<persistent_blocks((const void *)k_edt_batch, kEdtNT, tiles), kEdtNT, 0, s>>>(
+    constexpr size_t smem = EdtSmem<8, 8>::bytes;
+    k_edt_batch<<<persistent_blocks((const void *)k_edt_batch, kEdtNT, tiles, smem), kEdtNT, smem, s>>>(
         b, inMask, outMask, codes, signMask, counter);
 }
 

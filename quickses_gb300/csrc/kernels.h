@@ -13,7 +13,8 @@ void launch_atom_gather(const float *xyz, const float *r, const unsigned *skey, 
                         float4 *atoms, uint2 *cells, cudaStream_t s);
 void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigned *inMask, unsigned *outMask,
                 cudaStream_t s);
-// shape: refine tile of 8 x 8 (0) or 16 x 8 (1) z-rows; the same codes for both.
+// shape: refine tile of 8 x 8 (0), 16 x 8 (1), 16 x 16 (2) or 32 x 16 (3) z-rows; the same
+// codes for all.
 void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
                 unsigned *signMask, cudaStream_t s, int shape = 0);
 
@@ -73,7 +74,7 @@ int gs_shape_candidates(GsShape *out, int max);
 // Tuned refine tile shape (launch_edt `shape`) for grids of G voxels per axis, or 0.
 int edt_shape(int G);
 void edt_shape_record(int G, int shape);
-constexpr int kEdtShapes = 2;
+constexpr int kEdtShapes = 4;
 constexpr unsigned kGsSlabMaxVerts = 25000;
 
 // ---- batch forms (QBatch: per-molecule grids and offsets in device memory)

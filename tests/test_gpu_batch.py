@@ -130,7 +130,7 @@ def test_autotune_keeps_results(ctx):
     xyz, rad, _ = q.molecules.ball(2000, 45)
     before = ctx.compute(xyz, rad, voxel=0.4, smooth=1)
     threads, target, flags, field_shape, ms = ctx.autotune(xyz, rad, voxel=0.4, smooth=1)
-    assert threads in (512, 1024) and target >= 256 and 0 <= flags <= 15 and field_shape in (0, 1) and ms > 0
+    assert threads in (512, 1024) and target >= 256 and 0 <= flags <= 15 and field_shape in (0, 1, 2, 3) and ms > 0
     _same(ctx.compute(xyz, rad, voxel=0.4, smooth=1), before)
     reqs = [_req(*q.molecules.ball(n, 70 + n)[:2], 0.4, 1) for n in (700, 3000)]
     singles = [_single(ctx, r) for r in reqs]

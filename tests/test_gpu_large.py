@@ -31,11 +31,12 @@ def big():
     return xyz, rad, g, m0, codes, m1, m1k
 
 
-def test_field_16x8_tiles_match(big):
-    """The 16 x 8 refine tile gives the same 664^3 codes as the 8 x 8 one."""
+@pytest.mark.parametrize("shape", [1, 2, 3])
+def test_field_tile_shapes_match(big, shape):
+    """The 16 x 8, 16 x 16 and 32 x 16 refine tiles give the same 664^3 codes as the 8 x 8 one."""
     xyz, rad, g, _, codes, _, _ = big
     with q.Context(0) as c:
-        c.set_field_shape(1)
+        c.set_field_shape(shape)
         c.compute(xyz, rad, voxel=WL.voxel, smooth=0)
         assert np.array_equal(c.debug_codes(g.G), codes)
 

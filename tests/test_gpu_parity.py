@@ -63,10 +63,11 @@ def test_field_codes_exact(ctx, kind, n, seed, dx):
         mism[:5].tolist(), codes[tuple(mism[:5].T)].tolist(), ref[tuple(mism[:5].T)].tolist())
 
 
-@pytest.mark.parametrize("shape", [0, 1])
+@pytest.mark.parametrize("shape", [0, 1, 2, 3])
 @pytest.mark.parametrize("kind,n,seed,dx", CASES[1:])
 def test_field_codes_every_tile_shape(ctx, kind, n, seed, dx, shape):
-    """Both refine tile shapes (8 x 8 and 16 x 8 z-rows per CTA) give the oracle's codes."""
+    """Every refine tile shape (8 x 8, 16 x 8, 16 x 16, 32 x 16 z-rows per CTA) gives the
+    oracle's codes."""
     xyz, rad = _atoms(kind, n, seed)
     ctx.set_field_shape(shape)
     try:
