@@ -45,7 +45,8 @@ enum {
     QSES_ERR_OUT_OF_MEMORY = 4, /* device or pinned host allocation failed */
     QSES_ERR_UNSUPPORTED = 5,   /* input outside the supported envelope (see qses_status_string) */
     QSES_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up */
-    QSES_ERR_INTERNAL = 7       /* internal consistency check failed */
+    QSES_ERR_INTERNAL = 7,      /* internal consistency check failed */
+    QSES_ERR_CANCELLED = 8      /* a served request withdrawn before it ran (qses_server_cancel) */
 };
 
 /* --------------------------------------------- QuickSES-compatible library surface */
@@ -225,6 +226,10 @@ QSES_API int qses_server_wait(qses_server *s, unsigned long long ticket, double 
 /* [0] batches run, [1] requests served, [2] largest batch, [3] most lanes busy at once,
  * [4] requests queued now.  Returns the number of values written. */
 QSES_API int qses_server_stats(qses_server *s, unsigned long long *out, int max);
+/* Withdraws a request that is still queued: QSES_OK, and its qses_server_wait returns
+ * QSES_ERR_CANCELLED with an empty mesh.  A request already taken into a batch runs to the
+ * end: QSES_ERR_UNSUPPORTED.  An unknown or collected ticket: QSES_ERR_INVALID_ARG. */
+QSES_API int qses_server_cancel(qses_server *s, unsigned long long ticket);
 /* Finishes queued work, then frees everything (uncollected meshes included). */
 QSES_API int qses_server_destroy(qses_server *s);
 
@@ -253,6 +258,20 @@ QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int ma
  * (closest atom, filter, smoothing, downloads).  No reference counterpart.  Returns the
  * number of values written. */
 QSES_API int qses_host_timeline(qses_context *ctx, double *ms, int max);
+
+/* ------------------------------------------------------------- failure tests */
+
+/* Test hooks (no reference counterpart; QuickSES exits the process on any error).
+ * qses_debug_fail_reservations: the next n device workspace reservations of any context fail
+ * with QSES_ERR_OUT_OF_MEMORY, as an exhausted device would; the failing call returns that
+ * code and later calls on the same context work.
+ * qses_debug_wait_limit: runs the smoothing kernel on a 4-vertex mesh in which one vertex
+ * waits for a hand-off from a lower slab that never comes, with its wait limited to
+ * spin_cycles clock cycles (1e6 .. 4e9); *kernel_status receives the status the kernel wrote
+ * (QSES_ERR_TIMEOUT: the wait gave up and every CTA returned).  Returns QSES_OK when the
+ * kernel ran and the context is still usable. */
+QSES_API void qses_debug_fail_reservations(unsigned n);
+QSES_API int qses_debug_wait_limit(qses_context *ctx, long long spin_cycles, int *kernel_status);
 
 /* ------------------------------------------------------------------ CUDA graphs */
 

@@ -16,6 +16,7 @@ QSES_ERR_OUT_OF_MEMORY = 4
 QSES_ERR_UNSUPPORTED = 5
 QSES_ERR_TIMEOUT = 6
 QSES_ERR_INTERNAL = 7
+QSES_ERR_CANCELLED = 8
 QSES_FLAG_KEEP_DEGENERATE = 1
 
 
@@ -98,6 +99,7 @@ SIGNATURES = {
                                         ctypes.POINTER(TicketInfo)]),
     "qses_server_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
     "qses_server_destroy": (ctypes.c_int, [_VP]),
+    "qses_server_cancel": (ctypes.c_int, [_VP, ctypes.c_ulonglong]),
     "qses_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "qses_last_error": (ctypes.c_char_p, [_VP]),
     "qses_set_profiling": (ctypes.c_int, [_VP, ctypes.c_int]),
@@ -106,6 +108,8 @@ SIGNATURES = {
     "qses_last_download_bytes": (ctypes.c_ulonglong, [_VP]),
     "qses_diagnostics": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
     "qses_set_graphs": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "qses_debug_fail_reservations": (None, [ctypes.c_uint]),
+    "qses_debug_wait_limit": (ctypes.c_int, [_VP, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int)]),
     "qses_host_timeline": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "qses_debug_slab_plan": (ctypes.c_int, [ctypes.c_uint, _VP, _VP, ctypes.c_uint, ctypes.c_int, ctypes.c_uint,
                                             ctypes.c_uint, ctypes.c_uint, ctypes.c_int, _VP, _VP, ctypes.c_size_t]),

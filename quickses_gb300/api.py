@@ -379,6 +379,15 @@ class Server:
             self._lib.qses_mesh_release(ctypes.byref(m))
         return mesh, {"queued_s": info.queued_s, "run_s": info.run_s, "total_s": info.total_s}
 
+    def cancel(self, ticket):
+        """Withdraw a queued request (True); False when it is already running."""
+        rc = self._lib.qses_server_cancel(self._h, ctypes.c_ulonglong(ticket))
+        if rc == L.QSES_OK:
+            return True
+        if rc == 5:  # QSES_ERR_UNSUPPORTED: taken into a batch already
+            return False
+        raise QSESError(rc, "qses_server_cancel: %s" % L.status_string(rc))
+
     def stats(self):
         out = (ctypes.c_ulonglong * 5)()
         k = self._lib.qses_server_stats(self._h, out, 5)

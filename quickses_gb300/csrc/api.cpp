@@ -199,6 +199,7 @@ QSES_API const char *qses_status_string(int status) {
         case QSES_ERR_UNSUPPORTED: return "input outside the supported envelope";
         case QSES_ERR_TIMEOUT: return "bounded device wait timed out";
         case QSES_ERR_INTERNAL: return "internal error";
+        case QSES_ERR_CANCELLED: return "request cancelled";
         default: return "unknown status";
     }
 }
@@ -704,6 +705,56 @@ QSES_API int qses_debug_slab_plan(unsigned nv, const unsigned *mol_off, const in
         if (cap < pl.table.size()) return QSES_ERR_INVALID_ARG;
         memcpy(table, pl.table.data(), 4 * pl.table.size());
     }
+    return QSES_OK;
+}
+
+QSES_API void qses_debug_fail_reservations(unsigned n) { qses::g_fail_reserves.store(n); }
+
+QSES_API int qses_debug_wait_limit(qses_context *ctx, long long spin_cycles, int *kernel_status) {
+    if (!ctx || !kernel_status || spin_cycles < 1000000ll || spin_cycles > 4000000000ll) return QSES_ERR_INVALID_ARG;
+    *kernel_status = 0;
+    cudaSetDevice(ctx->device);
+    // Vertices 0-1 (slab 0) and 2-3 (slab 1), lists 0:{1} 1:{0} 2:{3} 3:{2}.  Vertex 2 is
+    // marked as waiting for one lower-slab hand-off (remote count 1, +1 in its counter) that
+    // no vertex ever sends, so slab 1 cannot finish and its boundary warp's wait runs out.
+    const unsigned table_h[6] = {2, 0, 2, 4, 0, 1};  // Q, bounds (qcap + 1 = 3), order
+    const uint2 start_h[5] = {{0, 0}, {1, 0}, {2, 0}, {3, 0}, {4, 0}};
+    const unsigned nbr_h[4] = {1, 0, 3, 2};
+    const unsigned short cnt_h[4] = {0, 1, 1, 1};
+    const int remote_h[4] = {0, 0, 1, 0};
+    const uint2 home_h[4] = {{0, 0}, {0, 0}, {1, 2}, {1, 2}};
+    const float4 pos_h[4] = {{0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}};
+    char *d = nullptr;
+    const size_t bytes = 4096;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "wait-limit check buffers");
+    }
+    unsigned *table = (unsigned *)d, *nbr = (unsigned *)(d + 256), *inbox = (unsigned *)(d + 512),
+             *tails = (unsigned *)(d + 768);
+    uint2 *start = (uint2 *)(d + 1024), *home = (uint2 *)(d + 1280);
+    unsigned short *cnt = (unsigned short *)(d + 1536);
+    int *remote = (int *)(d + 1792), *err = (int *)(d + 2048);
+    float4 *pos = (float4 *)(d + 2304);
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMemsetAsync(d, 0, bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(inbox, 0xff, 256, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(table, table_h, sizeof(table_h), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(start, start_h, sizeof(start_h), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(nbr, nbr_h, sizeof(nbr_h), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, cnt_h, sizeof(cnt_h), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(remote, remote_h, sizeof(remote_h), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(home, home_h, sizeof(home_h), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pos, pos_h, sizeof(pos_h), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = qses::launch_gs_slab(pos, 0, 4, 2, table, 2, tails + 2, home, 2, 512, 0, start, nbr, cnt, remote, inbox,
+                                 tails, err, spin_cycles, nullptr, s);
+    int h_err = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    if (e != cudaSuccess) return ctx->fail(QSES_ERR_CUDA, "wait-limit check", e);
+    *kernel_status = h_err;
     return QSES_OK;
 }
 

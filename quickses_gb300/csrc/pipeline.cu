@@ -6,6 +6,7 @@
 // context-owned workspace that is reused across calls, with four small count read-backs.
 // The mesh is the reference's single-slice result (its output for -s >= grid size).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -170,8 +171,13 @@ int gs_shape_candidates(GsShape *out, int max) {
 
 // ------------------------------------------------------------------ arena
 
+// Test hook: the next n workspace reservations fail as if the device were out of memory.
+std::atomic<unsigned> g_fail_reserves{0};
+
 int Arena::reserve(size_t bytes) {
     off = 0;
+    for (unsigned f = g_fail_reserves.load(); f > 0;)
+        if (g_fail_reserves.compare_exchange_weak(f, f - 1)) return QSES_ERR_OUT_OF_MEMORY;
     if (bytes <= cap) return QSES_OK;
     gen++;
     if (base) cudaFree(base);

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <chrono>
 #include <string>
 #include <utility>
@@ -11,6 +12,9 @@
 #include "qses_internal.h"
 
 namespace qses {
+
+// Test hook (qses_debug_fail_reservations): reservations left to fail.
+extern std::atomic<unsigned> g_fail_reserves;
 
 // Bump allocator over one device allocation that persists across calls.
 struct Arena {

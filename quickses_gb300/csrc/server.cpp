@@ -225,6 +225,26 @@ QSES_API int qses_server_wait(qses_server *s, unsigned long long ticket, double 
     return st;
 }
 
+QSES_API int qses_server_cancel(qses_server *s, unsigned long long ticket) {
+    if (!s) return QSES_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lock(s->mu);
+    auto it = s->jobs.find(ticket);
+    if (it == s->jobs.end()) return QSES_ERR_INVALID_ARG;
+    Job *j = it->second.get();
+    auto q = std::find(s->pending.begin(), s->pending.end(), j);
+    if (q == s->pending.end()) return QSES_ERR_UNSUPPORTED;  // in a batch already (or done)
+    s->pending.erase(q);
+    j->status = QSES_ERR_CANCELLED;
+    j->t_start = j->t_done = Clock::now();
+    j->done = true;
+    j->xyz.clear();
+    j->xyz.shrink_to_fit();
+    j->r.clear();
+    j->r.shrink_to_fit();
+    s->cv_done.notify_all();
+    return QSES_OK;
+}
+
 QSES_API int qses_server_stats(qses_server *s, unsigned long long *out, int max) {
     if (!s || !out) return 0;
     std::lock_guard<std::mutex> lock(s->mu);
