@@ -53,10 +53,11 @@ class ClockSampler:
     slows CUDA calls for a while), summarised over the samples stamped between mark() and
     stop(): the timed region."""
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, interval_ms=100):
         self.proc = None
         self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
         self.device = device
+        self.interval_ms = interval_ms
         self.t0 = self.t1 = None
 
     def start(self):
@@ -67,7 +68,8 @@ class ClockSampler:
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=timestamp,clocks.sm,clocks.max.sm,power.draw,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)], stdout=self.f,
+                stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         if self.proc:
@@ -430,16 +432,17 @@ def run_batch_form(args):
         stages = ctx.stage_times()
         launches = ctx.last_launch_count()
         ctx.set_profiling(False)
-        times = []
+        times, timelines = [], []
         clk.mark()
         for _ in range(args.steps):
             t0 = time.perf_counter()
             nv, nt, bad = _raw_batch(lib, L, ctx, rr, n)
             times.append(time.perf_counter() - t0)
+            timelines.append(ctx.host_timeline())
         clk.stop()
         sec = float(np.mean(times))
         graphs_timed = ctx.graph_stats()
-        timeline = ctx.host_timeline()
+        timeline = timelines[-1]
         _raw_single(lib, L, ctx, reqs[:8])
         t0 = time.perf_counter()
         _raw_single(lib, L, ctx, reqs)
@@ -463,6 +466,7 @@ def run_batch_form(args):
         "stages_ms": {k: round(v, 3) for k, v in stages}, "gpu_launches": launches * args.steps,
         "step_ms": [round(1e3 * t, 3) for t in times],
         "host_timeline_ms": {k: round(v, 3) for k, v in timeline.items()},
+        "step_timelines_ms": [{k: round(v, 2) for k, v in tl.items()} for tl in timelines],
         "clocks": clk.summary()}))
 
 

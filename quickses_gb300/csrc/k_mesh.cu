@@ -504,29 +504,80 @@ __global__ void k_tri_compact_batch(QBatch b, const unsigned *__restrict__ tri, 
 
 // --------------------------------------------------------------- smoothing
 
-// Neighbour-list offsets from the stably sorted corner occurrences: v's list starts at twice
-// the position of its first occurrence (two entries per occurrence); vertices between two
-// sorted keys (none in a welded mesh) get empty lists.
-__global__ void k_csr_offsets(const unsigned *__restrict__ skey, size_t n3, unsigned nv, uint2 *__restrict__ start) {
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n3) return;
-    const unsigned k = skey[p];
-    const long long prev = p ? (long long)skey[p - 1] : -1ll;
-    for (long long v = prev + 1; v <= (long long)k && v <= (long long)nv; v++) start[v] = make_uint2(2u * (unsigned)p, 0u);
-    if (p == n3 - 1)
-        for (long long v = (long long)k + 1; v <= (long long)nv; v++) start[v] = make_uint2(2u * (unsigned)n3, 0u);
+// Neighbour lists without a sort.  count: occurrences of each vertex among the 3T triangle
+// corners (start[v].x, later scanned); scatter: each corner q is written into its vertex's
+// range at a position taken with an atomic (start[v].y, zero after the scan), so the order
+// within a range is arbitrary; sortfill: one thread per vertex sorts its range by corner
+// index, which restores triangle order exactly (the order getNeighboorsVertices appends
+// in, SmoothMesh.cpp:45-66), writes the two other corners of each triangle to the list, and
+// doubles the offset (two entries per occurrence).
+__global__ void k_csr_count(const unsigned *__restrict__ tri, size_t n3, uint2 *__restrict__ start) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n3) atomicAdd(&start[tri[q]].x, 1u);
 }
 
-// Sorted occurrence p (vertex v, corner q = 3t + c in triangle order) contributes the two
-// other corners of triangle t to v's list, as getNeighboorsVertices appends them.
-__global__ void k_csr_fill(const unsigned *__restrict__ tri, const unsigned *__restrict__ socc, size_t n3,
-                           unsigned *__restrict__ nbr) {
-    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n3) return;
-    const unsigned q = socc[p], t = q / 3u, c = q - 3u * t;
-    const unsigned a = tri[3ull * t], b = tri[3ull * t + 1], d = tri[3ull * t + 2];
-    nbr[2 * p] = c == 0 ? b : a;
-    nbr[2 * p + 1] = c == 2 ? b : d;
+__global__ void k_csr_scatter(const unsigned *__restrict__ tri, size_t n3, uint2 *__restrict__ start,
+                              unsigned *__restrict__ occ) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n3) return;
+    const unsigned v = tri[q];
+    const unsigned k = atomicAdd(&start[v].y, 1u);
+    occ[start[v].x + k] = (unsigned)q;
+}
+
+__global__ void k_csr_sortfill(const unsigned *__restrict__ tri, unsigned *__restrict__ occ, size_t n3, unsigned nv,
+                               uint2 *__restrict__ start, unsigned *__restrict__ nbr) {
+    const unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v > nv) return;
+    if (v == nv) {
+        start[nv] = make_uint2(2u * (unsigned)n3, 0u);
+        return;
+    }
+    const uint2 st = start[v];
+    const unsigned o = st.x, n = st.y;  // offset, occurrences
+    constexpr unsigned kReg = 16;
+    if (n <= kReg) {
+        unsigned r[kReg];
+#pragma unroll
+        for (unsigned i = 0; i < kReg; i++) r[i] = i < n ? occ[o + i] : 0xffffffffu;
+        // insertion sort in registers (n is small: ~6 incident triangles per vertex)
+#pragma unroll
+        for (unsigned i = 1; i < kReg; i++) {
+#pragma unroll
+            for (unsigned j = i; j > 0; j--) {
+                const unsigned a = r[j - 1], b = r[j];
+                r[j - 1] = min(a, b);
+                r[j] = max(a, b);
+            }
+        }
+#pragma unroll
+        for (unsigned i = 0; i < kReg; i++) {
+            if (i < n) {
+                const unsigned q = r[i], t = q / 3u, c = q - 3u * t;
+                const unsigned a = tri[3ull * t], b = tri[3ull * t + 1], d = tri[3ull * t + 2];
+                nbr[2ull * (o + i)] = c == 0 ? b : a;
+                nbr[2ull * (o + i) + 1] = c == 2 ? b : d;
+            }
+        }
+    } else {
+        // rare high-degree vertex: insertion sort in place in global memory
+        for (unsigned i = 1; i < n; i++) {
+            const unsigned x = occ[o + i];
+            unsigned j = i;
+            while (j > 0 && occ[o + j - 1] > x) {
+                occ[o + j] = occ[o + j - 1];
+                j--;
+            }
+            occ[o + j] = x;
+        }
+        for (unsigned i = 0; i < n; i++) {
+            const unsigned q = occ[o + i], t = q / 3u, c = q - 3u * t;
+            const unsigned a = tri[3ull * t], b = tri[3ull * t + 1], d = tri[3ull * t + 2];
+            nbr[2ull * (o + i)] = c == 0 ? b : a;
+            nbr[2ull * (o + i) + 1] = c == 2 ? b : d;
+        }
+    }
+    start[v] = make_uint2(2u * o, 0u);
 }
 
 __device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
@@ -1008,11 +1059,15 @@ void launch_tri_flags(const unsigned *tri, unsigned nt, uint2 *flags, cudaStream
 void launch_tri_compact(const unsigned *tri, unsigned nt, const uint2 *excl, unsigned *out, cudaStream_t s) {
     k_tri_compact<<<nblk(nt, 256), 256, 0, s>>>(tri, nt, excl, out);
 }
-void launch_csr_offsets(const unsigned *skey, size_t n3, unsigned nv, uint2 *start, cudaStream_t s) {
-    k_csr_offsets<<<nblk(n3, 256), 256, 0, s>>>(skey, n3, nv, start);
+void launch_csr_count(const unsigned *tri, size_t n3, uint2 *start, cudaStream_t s) {
+    k_csr_count<<<nblk(n3, 256), 256, 0, s>>>(tri, n3, start);
 }
-void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s) {
-    k_csr_fill<<<nblk(n3, 256), 256, 0, s>>>(tri, socc, n3, nbr);
+void launch_csr_scatter(const unsigned *tri, size_t n3, uint2 *start, unsigned *occ, cudaStream_t s) {
+    k_csr_scatter<<<nblk(n3, 256), 256, 0, s>>>(tri, n3, start, occ);
+}
+void launch_csr_sortfill(const unsigned *tri, unsigned *occ, size_t n3, unsigned nv, uint2 *start, unsigned *nbr,
+                         cudaStream_t s) {
+    k_csr_sortfill<<<nblk((size_t)nv + 1, 128), 128, 0, s>>>(tri, occ, n3, nv, start, nbr);
 }
 void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsigned v1, const unsigned *table,
                      unsigned short *cnt_local, int *remote, uint2 *home, cudaStream_t s) {

@@ -29,9 +29,13 @@ void launch_closest(const QGrid &g, const float *vq, unsigned nv, const float4 *
                     const unsigned *sorted_to_input, int *asorted, int *ainput, cudaStream_t s);
 void launch_tri_flags(const unsigned *tri, unsigned nt, uint2 *flags, cudaStream_t s);
 void launch_tri_compact(const unsigned *tri, unsigned nt, const uint2 *excl, unsigned *out, cudaStream_t s);
-// start[v].x (v <= nv) from the stably sorted corner vertex ids skey
-void launch_csr_offsets(const unsigned *skey, size_t n3, unsigned nv, uint2 *start, cudaStream_t s);
-void launch_csr_fill(const unsigned *tri, const unsigned *socc, size_t n3, unsigned *nbr, cudaStream_t s);
+// Neighbour lists by counting: start (nv + 1 entries, zeroed) -> counts -> (scan) -> corner
+// occurrences scattered per vertex into occ (n3) -> sorted per vertex and expanded into nbr
+// (2 n3), start[v].x = list offset.
+void launch_csr_count(const unsigned *tri, size_t n3, uint2 *start, cudaStream_t s);
+void launch_csr_scatter(const unsigned *tri, size_t n3, uint2 *start, unsigned *occ, cudaStream_t s);
+void launch_csr_sortfill(const unsigned *tri, unsigned *occ, size_t n3, unsigned nv, uint2 *start, unsigned *nbr,
+                         cudaStream_t s);
 // Slab table of one Gauss-Seidel wave (device words): [0] Q slabs, [1, Q + 2) their bounds in
 // id order (qcap + 1 slots), [qcap + 2, qcap + 2 + Q) the slab ids in the order CTAs take them.
 inline size_t gs_table_words(unsigned qcap) { return 2ull * qcap + 2; }

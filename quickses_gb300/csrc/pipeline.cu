@@ -510,7 +510,7 @@ struct FinishSeg {
     char *h_dl;            // pinned host mesh block, or null
     unsigned long long dl_vb, dl_tb, dl_ab;
     uint2 *deg;
-    unsigned *okey, *okey2, *oval, *oval2, *nbr;
+    unsigned *okey, *nbr;  // okey: the corners scattered per vertex
     void *tmpb;
     float4 *pos4;
     unsigned short *cnt;
@@ -565,14 +565,16 @@ static int enqueue_finish(qses_context *ctx, const FinishSeg &c, SegOut &o) {
 
     // Gauss-Seidel smoothing on the device
     if (c.passes > 0 && c.nv > 0 && c.nt > 0) {
-        // neighbour lists: the 3T corners stably sorted by vertex (the triangle order within a
-        // vertex is the order getNeighboorsVertices appends in), offsets from the sorted keys
-        QCHK(radix_sort<unsigned>(c.okey, c.okey2, c.oval, c.oval2, (unsigned)c.n3, bits_for(c.nv - 1), true, c.tmpb,
-                                  c.err, s, &ctx->launches, &o.alt, c.tri));
-        const unsigned *socc = o.alt ? c.oval2 : c.oval, *skey = o.alt ? c.okey2 : c.okey;
-        launch_csr_offsets(skey, c.n3, c.nv, c.deg, s);
+        // neighbour lists: count the corners per vertex, scan, scatter them per vertex, then
+        // sort each vertex's few corners back into triangle order (the order
+        // getNeighboorsVertices appends in) and expand them into the lists
+        QCHK(cudaMemsetAsync(c.deg, 0, 8ull * (c.nv + 1), s));
+        launch_csr_count(c.tri, c.n3, c.deg, s);
         ctx->launches++;
-        launch_csr_fill(c.tri, socc, c.n3, c.nbr, s);
+        QCHK(scan_u2(c.deg, c.deg, c.nv + 1, nullptr, c.tmpb, c.err, s, &ctx->launches));
+        launch_csr_scatter(c.tri, c.n3, c.deg, c.okey, s);
+        ctx->launches++;
+        launch_csr_sortfill(c.tri, c.okey, c.n3, c.nv, c.deg, c.nbr, s);
         ctx->launches++;
         ctx->mark("smooth_csr");
         // the closest-atom pass on the side stream reads the welded positions in vq
@@ -697,8 +699,8 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
                             scan_u2_tmp_bytes(NE), scan_u2_tmp_bytes(T), scan_u2_tmp_bytes(NE + 1)});
     const size_t nflag = std::max<size_t>((size_t)NE + 1, (size_t)T) + 1;
     size_t needB = 2 * align256(4 * n3) + 2 * align256(8ull * NE) + 2 * align256(4ull * NE) + align256(8ull * nflag) +
-                   align256(4ull * NE) + align256(12ull * NE) + 2 * align256(4ull * NE) + 2 * align256(4 * n3) +
-                   2 * align256(4 * n3) + align256(8 * n3) + 3 * align256(4ull * NE) + 4096 +
+                   align256(4ull * NE) + align256(12ull * NE) + 2 * align256(4ull * NE) + align256(4 * n3 + 4) +
+                   align256(8 * n3) + 3 * align256(4ull * NE) + 4096 +
                    align256(16ull * NE + 16) +
                    align256(tmpB) + align256(8ull * T + 16) + align256(scan_u2_tmp_bytes(T + 1)) + 4096;
     if (ctx->mesh_ws.reserve(needB) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "mesh workspace");
@@ -711,8 +713,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     unsigned *vmap = (unsigned *)B.take(4ull * NE + 4);
     float *vq = (float *)B.take(12ull * NE + 12);
     int *asorted = (int *)B.take(4ull * NE + 4), *ainput = (int *)B.take(4ull * NE + 4);
-    unsigned *okey = (unsigned *)B.take(4 * n3 + 4), *okey2 = (unsigned *)B.take(4 * n3 + 4);
-    unsigned *oval = (unsigned *)B.take(4 * n3 + 4), *oval2 = (unsigned *)B.take(4 * n3 + 4);
+    unsigned *okey = (unsigned *)B.take(4 * n3 + 4);
     unsigned *nbr = (unsigned *)B.take(8 * n3 + 8);
     int *lower = (int *)B.take(4ull * NE + 4), *cnt = (int *)B.take(4ull * NE + 4);
     float4 *pos4 = (float4 *)B.take(16ull * NE + 16);
@@ -793,9 +794,6 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     }
     c.deg = flags;  // reuse: nv + 1 <= NE + 1 entries
     c.okey = okey;
-    c.okey2 = okey2;
-    c.oval = oval;
-    c.oval2 = oval2;
     c.nbr = nbr;
     c.tmpb = tmpb;
     c.pos4 = pos4;
