@@ -470,25 +470,50 @@ def run_batch_form(args):
         "clocks": clk.summary()}))
 
 
+def _raw_wait(lib, L, srv, ticket):
+    """One result through the C-ABI (qses_server_wait + qses_mesh_release, the mesh stays in
+    its pinned block: no copy into Python arrays); returns its submit-to-result time (s)."""
+    m, info = L.Mesh(), L.TicketInfo()
+    rc = lib.qses_server_wait(srv.handle, ctypes.c_ulonglong(ticket), -1.0, ctypes.byref(m), ctypes.byref(info))
+    lib.qses_mesh_release(ctypes.byref(m))
+    if rc != 0:
+        raise RuntimeError("served request failed: %d" % rc)
+    return info.total_s
+
+
 def run_served_form(args):
     """Served form: open-loop Poisson arrivals into qses_server (continuous batching over
     `lanes` streams, 120 GB admission budget); per offered rate, p50/p99 of submit-to-result
     latency and the completed-request rate.  Requests: atom counts log-uniform in
-    [200, 200000], voxel one of {0.3, 0.4, 0.5} A, 1 pass, drawn from 160 seeded molecules."""
+    [200, 200000], voxel one of {0.3, 0.4, 0.5} A, 1 pass, drawn from 160 seeded molecules.
+    Results are taken through the C-ABI without copying the meshes into Python."""
     import threading
     import quickses_gb300 as q
+    from quickses_gb300 import _lib as L
+    lib = L.lib()
     rates = [float(x) for x in args.rates.split(",")]
     per_rate = args.requests
     reqs = q.molecules.served_stream(per_rate * len(rates) + 64)
     rng = np.random.default_rng(11)
     sweep = []
     clk = ClockSampler(0).start()
-    with q.Context(0) as tctx:  # launch-shape tuning on a sample (process-wide, like a service start)
-        tune = tctx.autotune_batch(reqs[-64:-32])
+    if args.served_shape:  # a fixed process-wide shape for the lanes (e.g. one that shares the SMs)
+        th, tg, fl = [int(x) for x in args.served_shape.split(",")]
+        from quickses_gb300 import _lib as L0
+        if L0.lib().qses_set_default_smoothing_shape(1, th, tg, fl) != 0:
+            raise SystemExit("bad --served-shape")
+        tune = (th, tg, fl, 0.0)
+    else:
+        with q.Context(0) as tctx:  # launch-shape tuning on a sample (process-wide, like a service start)
+            tune = tctx.autotune_batch(reqs[-64:-32])
     with q.Server(lanes=args.lanes, memory_budget=120 << 30, max_batch=256,
                   max_batch_voxels=int(args.batch_voxels) if args.batch_voxels else None) as srv:
-        for r in reqs[-64:]:  # warm-up: workspaces and pinned blocks grow to size once
-            srv.wait(srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"]))
+        # warm-up: a burst, so that batches as large as the timed ones form and workspaces and
+        # pinned blocks grow to size before the timed phases
+        for _ in range(2):
+            warm = [srv.submit(r["xyz"], r["radii"], r["voxel"], r["smooth"]) for r in reqs[-64:]]
+            for t in warm:
+                _raw_wait(lib, L, srv, t)
         clk.mark()
         for ri, rate in enumerate(rates):
             chunk = reqs[ri * per_rate:(ri + 1) * per_rate]
@@ -510,8 +535,7 @@ def run_served_form(args):
             for k in range(per_rate):
                 while tickets[k] is None:
                     time.sleep(0.0002)
-                _, info = srv.wait(tickets[k])
-                lat.append(info["total_s"])
+                lat.append(_raw_wait(lib, L, srv, tickets[k]))
             t_end = time.perf_counter()
             th.join()
             lat = np.array(lat) * 1e3
@@ -531,7 +555,7 @@ def run_served_form(args):
     best = max(sweep, key=lambda x: x["achieved_per_s"])
     print(json.dumps({
         "metric": "SES molecules/s (served form)", "value": best["achieved_per_s"], "unit": "molecules/s",
-        "n_gpus": 1, "steps": len(rates), "warmup": 64, "ms_per_step": None, "higher_is_better": True,
+        "n_gpus": 1, "steps": len(rates), "warmup": 128, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": "open-loop Poisson, %d requests per offered rate, atom counts log-uniform in "
                                "[200, 200000], voxel one of {0.3, 0.4, 0.5} A, 1 pass" % per_rate,
@@ -560,6 +584,8 @@ def main():
     ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="served form: offered requests/s")
     ap.add_argument("--requests", type=int, default=1000, help="served form: requests per offered rate")
     ap.add_argument("--lanes", type=int, default=2, help="served form: batches in flight")
+    ap.add_argument("--served-shape", default="",
+                    help="served form: smoothing shape threads,target,cache_flags for every lane (default: tuned)")
     ap.add_argument("--batch-voxels", type=float, default=0,
                     help="served form: grid voxels per batch (0 = the server's default)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")

@@ -187,6 +187,11 @@ QSES_API int qses_set_field_shape(qses_context *ctx, int shape);
  * Every shape gives the same mesh. */
 QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags,
                                       unsigned wave_vertices);
+/* Sets the process-wide smoothing shape (as qses_set_smoothing_shape, no waves) for every
+ * mesh size, of single-molecule calls (batch = 0) or of batch calls and server lanes
+ * (batch = 1), replacing what the autotuner recorded; contexts with a fixed shape keep it.
+ * No reference counterpart.  Lets a server use a shape that shares the SMs between lanes. */
+QSES_API int qses_set_default_smoothing_shape(int batch, int threads, unsigned target, unsigned cache_flags);
 /* The same for the batch form, timing whole qses_compute_batch calls on `reqs`. */
 QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, unsigned count, int repeats,
                                  int *threads_out, unsigned *target_out, unsigned *flags_out, float *ms_out);

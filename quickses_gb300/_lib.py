@@ -89,6 +89,7 @@ SIGNATURES = {
                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),
                                      ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_int), _FP]),
     "qses_set_field_shape": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "qses_set_default_smoothing_shape": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.c_uint]),
     "qses_autotune_batch": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.c_uint, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),
                                            ctypes.POINTER(ctypes.c_uint), _FP]),

@@ -357,6 +357,10 @@ class Server:
             raise QSESError(rc, "qses_server_create: " + L.status_string(rc))
         self._h = h
 
+    @property
+    def handle(self):
+        return self._h
+
     def submit(self, xyz, radii, voxel=0.5, smooth=1, keep_degenerate=False):
         xyz, radii = _f32(xyz, 3), _f32(radii)
         r = L.Request(xyz.ctypes.data, radii.ctypes.data, xyz.shape[0], float(voxel), int(smooth),

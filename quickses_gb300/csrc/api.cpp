@@ -531,6 +531,13 @@ QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned t
     return QSES_OK;
 }
 
+QSES_API int qses_set_default_smoothing_shape(int batch, int threads, unsigned target, unsigned cache_flags) {
+    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 15 || (cache_flags & qses::kGsPersistL2))
+        return QSES_ERR_INVALID_ARG;
+    qses::gs_shape_record_all(batch != 0, qses::GsShape{threads, target, cache_flags, 0});
+    return QSES_OK;
+}
+
 QSES_API int qses_set_field_shape(qses_context *ctx, int shape) {
     if (!ctx || shape < -1 || shape >= qses::kEdtShapes) return QSES_ERR_INVALID_ARG;
     ctx->edt_force = shape;

@@ -74,6 +74,7 @@ void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes);
 // Tuned shape for a mesh of nv vertices (batch = waves of many molecules), or the default.
 GsShape gs_shape(unsigned nv, bool batch);
 void gs_shape_record(unsigned nv, bool batch, GsShape s);
+void gs_shape_record_all(bool batch, GsShape s);  // every mesh-size class
 int gs_shape_candidates(GsShape *out, int max);
 // Tuned refine tile shape (launch_edt `shape`) for grids of G voxels per axis, or 0.
 int edt_shape(int G);

@@ -138,6 +138,14 @@ void gs_shape_record(unsigned nv, bool batch, GsShape sh) {
     g_tuned[batch][b] = true;
 }
 
+void gs_shape_record_all(bool batch, GsShape sh) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    for (int b = 0; b < 33; b++) {
+        g_tune[batch][b] = sh;
+        g_tuned[batch][b] = true;
+    }
+}
+
 static int g_edt_tune[2][16];  // [tuned?][log2 G]
 
 int edt_shape(int G) {
