@@ -98,13 +98,17 @@ __device__ __forceinline__ unsigned grp_incl_scan(unsigned v, int sub, int Lg) {
 // calls this (groups whose row is past the end pass valid = false and write nothing).
 // Edge keys get `keyhi` added (the molecule's slot above the local key bits in a batch, 0
 // for a single molecule).
+// Words per lane record of the triangle pass (34 used; an odd stride spreads the lanes'
+// writes over the shared-memory banks).
+constexpr int kRecW = 35;
+
 template <bool EMIT, bool FULL>
 __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid, int Lg,
                                        const unsigned *__restrict__ sign, const unsigned char *__restrict__ codes,
                                        const float *lut, const unsigned long long *s_tab,
                                        uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
                                        unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey,
-                                       unsigned long long keyhi) {
+                                       unsigned long long keyhi, unsigned *s_rec) {
     // FULL: one row per warp (Lg = 32, every group valid), known at compile time.
     if (FULL) {
         Lg = 32;
@@ -147,13 +151,19 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
         const unsigned Y00 = j < Gc ? (S00 ^ S01) & kv : 0u;
         const unsigned Z00 = (S00 ^ P00) & kc;
         const unsigned c00 = __popc(X00) + __popc(Y00) + __popc(Z00);
-        unsigned cellm = 0u, ntri = 0u;
+        unsigned cellm = 0u, ntri = 0u, nt0 = 0u, nt1 = 0u, nt2 = 0u;  // nt bit k of each active cell
         if (cellsRow) {
             cellm = ((S00 ^ S10) | (S00 ^ S11) | (S00 ^ S01) | (S00 ^ P00) | (S00 ^ P10) | (S00 ^ P11) |
                      (S00 ^ P01)) & kc;
             for (unsigned m = cellm; m; m &= m - 1u) {
                 unsigned b = __ffs(m) - 1;
-                ntri += (unsigned)(s_tab[cube_index(b, S00, S10, S11, S01, P00, P10, P11, P01)] >> 60);
+                const unsigned nt = (unsigned)(s_tab[cube_index(b, S00, S10, S11, S01, P00, P10, P11, P01)] >> 60);
+                ntri += nt;
+                if (EMIT) {
+                    nt0 |= (nt & 1u) << b;
+                    nt1 |= ((nt >> 1) & 1u) << b;
+                    nt2 |= ((nt >> 2) & 1u) << b;
+                }
             }
         }
         if (!EMIT) {
@@ -227,36 +237,68 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
                 }
             }
         }
-        // Triangles in cell order, corners as pre-weld vertex slots.
+        // Triangles in cell order, corners as pre-weld vertex slots.  The few words a surface
+        // crosses hold all of a row's cells, so the row's active cells are dealt out over the
+        // group's lanes: every lane publishes its word's sign words, edge masks, slot bases and
+        // per-cell triangle counts, and lane `sub` takes the row's active cells sub, sub + Lg,
+        // ...; a cell's first triangle is its word's first plus the counts of the cells below.
         {
-            unsigned ts = triBase + triCarry + tp;
-            for (unsigned m = cellm; m; m &= m - 1u) {
-                const unsigned b = __ffs(m) - 1;
-                const unsigned long long e = s_tab[cube_index(b, S00, S10, S11, S01, P00, P10, P11, P01)];
-                const unsigned nt = (unsigned)(e >> 60);
-                for (unsigned q = 0; q < 3 * nt; q++) {
-                    const unsigned edge = (unsigned)(e >> (4 * q)) & 15u;
-                    const unsigned own = (unsigned)(kEdgeOwner >> (5 * edge)) & 31u;
-                    const int o = (int)((own & 1u) * 2 + ((own >> 1) & 1u));  // (di, dj) -> owner index
-                    const unsigned dk = (own >> 2) & 1u, ax = own >> 3;
-                    const unsigned Xo = sel4(o, X00, X01, X10, X11), Yo = sel4(o, Y00, Y01, Y10, Y11);
-                    const unsigned Zo = sel4(o, Z00, Z01, Z10, Z11);
-                    unsigned slot = sel4(o, eb0 + ec0 + p0, eb1 + ec1 + p1, eb2 + ec2 + p2, eb3 + ec3 + p3);
-                    const unsigned vb = b + dk;
-                    if (vb < 32) {
-                        const unsigned lt = (1u << vb) - 1u;
-                        slot += __popc(Xo & lt) + __popc(Yo & lt) + __popc(Zo & lt);
-                        if (ax >= 1) slot += (Xo >> vb) & 1u;
-                        if (ax >= 2) slot += (Yo >> vb) & 1u;
-                    } else {
-                        slot += sel4(o, c00, c01, c10, c11);
-                        if (ax >= 1) slot += sel4(o, xn0, xn1, xn2, xn3);
-                        if (ax >= 2) slot += sel4(o, yn0, yn1, yn2, yn3);
-                    }
-                    tri[3ull * ts + q] = slot;
+            unsigned *my = s_rec + (threadIdx.x & 31) * kRecW;
+            my[0] = S00; my[1] = S10; my[2] = S11; my[3] = S01;
+            my[4] = P00; my[5] = P10; my[6] = P11; my[7] = P01;
+            my[8] = X00; my[9] = Y00; my[10] = Z00; my[11] = X01; my[12] = Y01; my[13] = Z01;
+            my[14] = X10; my[15] = Y10; my[16] = Z10; my[17] = X11; my[18] = Y11; my[19] = Z11;
+            my[20] = eb0 + ec0 + p0; my[21] = eb1 + ec1 + p1; my[22] = eb2 + ec2 + p2; my[23] = eb3 + ec3 + p3;
+            my[24] = c00; my[25] = c01; my[26] = c10; my[27] = c11;
+            my[28] = xn0 | (yn0 << 1) | (xn1 << 2) | (yn1 << 3) | (xn2 << 4) | (yn2 << 5) | (xn3 << 6) | (yn3 << 7);
+            my[29] = nt0; my[30] = nt1; my[31] = nt2; my[32] = cellm; my[33] = triBase + triCarry + tp;
+            __syncwarp();
+            const unsigned nc = __popc(cellm);
+            const unsigned cp = grp_incl_scan(nc, sub, Lg) - nc;
+            const unsigned ctot = grp_sum(nc, Lg);
+            const unsigned cmax = FULL ? ctot : __reduce_max_sync(0xffffffffu, ctot);  // warp-uniform
+            const int gbase = (int)(threadIdx.x & 31) & ~(Lg - 1);
+            for (unsigned cb = 0; cb < cmax; cb += (unsigned)Lg) {
+                const unsigned ci = cb + (unsigned)sub;
+                int lo = 0;
+                for (int step = Lg >> 1; step > 0; step >>= 1) {
+                    const unsigned pl = __shfl_sync(0xffffffffu, cp, gbase + lo + step);
+                    if (pl <= ci) lo += step;
                 }
-                ts += nt;
+                const unsigned po = __shfl_sync(0xffffffffu, cp, gbase + lo);
+                if (ci < ctot) {
+                    const unsigned *R = s_rec + (gbase + lo) * kRecW;
+                    const unsigned cm = R[32], r = ci - po;
+                    int b = 0;  // the r-th active cell of the owner's word: the largest b with r cells below
+                    for (int step = 16; step > 0; step >>= 1)
+                        if ((unsigned)__popc(cm & ((1u << (b + step)) - 1u)) <= r) b += step;
+                    const unsigned lt = (1u << b) - 1u;
+                    const unsigned ts = R[33] + __popc(R[29] & lt) + 2u * __popc(R[30] & lt) + 4u * __popc(R[31] & lt);
+                    const unsigned long long e = s_tab[cube_index(b, R[0], R[1], R[2], R[3], R[4], R[5], R[6], R[7])];
+                    const unsigned nt = (unsigned)(e >> 60);
+                    for (unsigned q = 0; q < 3 * nt; q++) {
+                        const unsigned edge = (unsigned)(e >> (4 * q)) & 15u;
+                        const unsigned own = (unsigned)(kEdgeOwner >> (5 * edge)) & 31u;
+                        const int o = (int)((own & 1u) * 2 + ((own >> 1) & 1u));  // (di, dj) -> owner index
+                        const unsigned dk = (own >> 2) & 1u, ax = own >> 3;
+                        const unsigned Xo = R[8 + 3 * o], Yo = R[9 + 3 * o], Zo = R[10 + 3 * o];
+                        unsigned slot = R[20 + o];
+                        const unsigned vb = (unsigned)b + dk;
+                        if (vb < 32) {
+                            const unsigned lt2 = (1u << vb) - 1u;
+                            slot += __popc(Xo & lt2) + __popc(Yo & lt2) + __popc(Zo & lt2);
+                            if (ax >= 1) slot += (Xo >> vb) & 1u;
+                            if (ax >= 2) slot += (Yo >> vb) & 1u;
+                        } else {
+                            slot += R[24 + o];
+                            if (ax >= 1) slot += (R[28] >> (2 * o)) & 1u;
+                            if (ax >= 2) slot += (R[28] >> (2 * o + 1)) & 1u;
+                        }
+                        tri[3ull * ts + q] = slot;
+                    }
+                }
             }
+            __syncwarp();  // the records are read before the next words' are written
         }
         triCarry += grp_sum(ntri, Lg);
         ec0 += grp_sum(c00, Lg);
@@ -274,6 +316,7 @@ __global__ void __launch_bounds__(256, 3) k_mc(QGrid g, const unsigned *__restri
                                             unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey) {
     __shared__ unsigned long long s_tab[256];
     __shared__ float s_lut[256];
+    __shared__ unsigned s_rec[EMIT ? 8 * 32 * kRecW : 1];  // per warp: one record per lane
     s_tab[threadIdx.x] = c_mc[threadIdx.x];
     if (EMIT) s_lut[threadIdx.x] = lut[threadIdx.x];
     __syncthreads();
@@ -281,7 +324,8 @@ __global__ void __launch_bounds__(256, 3) k_mc(QGrid g, const unsigned *__restri
     const long long first = ((long long)blockIdx.x * 8 + (threadIdx.x >> 5)) * (32 / Lg), nrow = (long long)E * E;
     if (first >= nrow) return;  // the whole warp
     const long long row = first + (threadIdx.x & 31) / Lg;
-    mc_row<EMIT, FULL>(g, row, row < nrow, Lg, sign, codes, s_lut, s_tab, rowCount, rowBase, tri, vkey, 0ull);
+    mc_row<EMIT, FULL>(g, row, row < nrow, Lg, sign, codes, s_lut, s_tab, rowCount, rowBase, tri, vkey, 0ull,
+                       s_rec + (EMIT ? (threadIdx.x >> 5) * 32 * kRecW : 0));
 }
 
 // Batch form: rows are numbered molecule after molecule, so one scan over all rows gives
@@ -293,8 +337,10 @@ __global__ void __launch_bounds__(256, 2) k_mc_batch(QBatch b, const unsigned *_
                                                   const uint2 *__restrict__ rowBase, unsigned *__restrict__ tri,
                                                   unsigned long long *__restrict__ vkey) {
     __shared__ unsigned long long s_tab[256];
+    __shared__ unsigned s_rec[EMIT ? 8 * 32 * kRecW : 1];  // per warp: one record per lane
     s_tab[threadIdx.x] = c_mc[threadIdx.x];
     __syncthreads();
+    unsigned *rec = s_rec + (EMIT ? (threadIdx.x >> 5) * 32 * kRecW : 0);
     const unsigned unit = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (unit >= __ldg(b.mc_unit_off + b.n_mol)) return;  // the whole warp
     const unsigned m = qses_find(b.mc_unit_off, b.n_mol, unit);
@@ -306,11 +352,11 @@ __global__ void __launch_bounds__(256, 2) k_mc_batch(QBatch b, const unsigned *_
     if (Lg == 32)  // warp-uniform
         mc_row<EMIT, true>(g, (long long)row, true, 32, sign + mol.mask_off, codes + mol.code_off,
                            b.lut + 256ull * m, s_tab, rowCount + r0, rowBase + r0, tri, vkey,
-                           (unsigned long long)m << b.key_bits);
+                           (unsigned long long)m << b.key_bits, rec);
     else
         mc_row<EMIT, false>(g, (long long)row, row < nrow, Lg, sign + mol.mask_off, codes + mol.code_off,
                             b.lut + 256ull * m, s_tab, rowCount + r0, rowBase + r0, tri, vkey,
-                            (unsigned long long)m << b.key_bits);
+                            (unsigned long long)m << b.key_bits, rec);
 }
 
 // ------------------------------------------------------------------ weld
