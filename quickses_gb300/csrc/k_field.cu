@@ -244,7 +244,8 @@ struct EdtSmem {
 template <int TX, int TY>
 __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, const unsigned *__restrict__ inMask,
                                          const unsigned *__restrict__ outMask, unsigned char *__restrict__ codes,
-                                         unsigned *__restrict__ signMask) {
+                                         unsigned *__restrict__ signMask,
+                                         const unsigned char *__restrict__ zd = nullptr) {
     using L = EdtSmem<TX, TY>;
     constexpr int HYM = L::HYM;
     extern __shared__ __align__(16) unsigned char edt_smem[];
@@ -276,7 +277,33 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
     }
     const int has_border = __syncthreads_or(anyb);
     int has_out = 0;
-    if (has_border) {
+    if (has_border && zd) {
+        // z distances computed once per voxel by k_edt_z: load the halo rows' bytes
+        int any = 0;
+        for (int q = t; q < HX * HY * 2; q += kEdtNT) {
+            const int row = q >> 1, half = q & 1;
+            const int i = i0 - R + row / HY, j = j0 - R + row % HY;
+            uint4 v = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+            if (i >= 0 && i < G && j >= 0 && j < G)
+                v = __ldg(reinterpret_cast<const uint4 *>(zd + ((size_t)i * G + j) * g.Gp + (size_t)k0) + half);
+            reinterpret_cast<uint4 *>(s_g[row])[half] = v;
+            any |= (v.x & v.y & v.z & v.w) != 0xffffffffu;
+        }
+        has_out = __syncthreads_or(any);
+        if (has_out) {
+            // y: min over dj of dj^2 + g^2 (<= 2 R^2 = 162 < 255), four voxels per word.
+            for (int q = t; q < HX * TY * 8; q += kEdtNT) {
+                const int w4 = q & 7, y = (q >> 3) % TY, hx = (q >> 3) / TY;
+                unsigned best = 0xffffffffu;
+                for (int dj = -R; dj <= R; dj++) {
+                    const unsigned gw = reinterpret_cast<const unsigned *>(s_g[hx * HY + y + R + dj])[w4];
+                    best = __vminu4(best, __vaddus4(gw, (unsigned)(dj * dj) * 0x01010101u));
+                }
+                reinterpret_cast<unsigned *>(s_h[hx][y])[w4] = best;
+            }
+            __syncthreads();
+        }
+    } else if (has_border) {
         int any = 0;
         for (int q = t; q < HX * HY; q += kEdtNT) {
             int i = i0 - R + q / HY, j = j0 - R + q % HY;
@@ -292,7 +319,7 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
         }
         has_out = __syncthreads_or(any);
     }
-    if (has_border && has_out) {
+    if (has_border && has_out && !zd) {
         // z: squared distance (in voxels, <= R^2) to the nearest outside voxel along the row.
         for (int q = t; q < HX * HY * 32; q += kEdtNT) {
             const int row = q >> 5, b = q & 31;
@@ -362,11 +389,64 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
     }
 }
 
+// z pass of the refine, once per voxel: squared distance (in voxels, <= R^2, 255 = none) to
+// the nearest outside voxel along the z row within the R window, one thread per 32-voxel
+// word (same values as the per-bit pass inside edt_tile).  zd has the codes' layout.
+__device__ __forceinline__ void edt_z_word(const QGrid &g, size_t q, const unsigned *__restrict__ outMask,
+                                           unsigned char *__restrict__ zd) {
+    const size_t row = q / g.W;
+    const int w = (int)(q - row * g.W), W = g.W, R = g.R;
+    const size_t base = row * W;
+    const unsigned a = w > 0 ? __ldg(outMask + base + w - 1) : 0u, c = __ldg(outMask + base + w),
+                   d = w + 1 < W ? __ldg(outMask + base + w + 1) : 0u;
+    unsigned out[8];
+    if ((a | c | d) == 0u) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) out[k] = 0xffffffffu;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            unsigned word = 0u;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int bit = 4 * k + e;
+                const unsigned long long up = (((unsigned long long)d << 32) | c) >> bit;
+                const int du = up ? (__ffsll((long long)up) - 1) : 1000;
+                const unsigned long long dn = (((unsigned long long)c << 32) | a) << (31 - bit);
+                const int dd = dn ? __clzll((long long)dn) : 1000;
+                const int m = min(du, dd);
+                word |= (m <= R ? (unsigned)(m * m) : 255u) << (8 * e);
+            }
+            out[k] = word;
+        }
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(zd + row * g.Gp + (size_t)w * 32);
+    dst[0] = make_uint4(out[0], out[1], out[2], out[3]);
+    dst[1] = make_uint4(out[4], out[5], out[6], out[7]);
+}
+
+__global__ void __launch_bounds__(256) k_edt_z(QGrid g, const unsigned *__restrict__ outMask,
+                                               unsigned char *__restrict__ zd) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < (size_t)g.G * g.G * g.W) edt_z_word(g, q, outMask, zd);
+}
+
+// Batch form: one thread per mask word of every molecule.
+__global__ void __launch_bounds__(256) k_edt_z_batch(QBatch b, unsigned words, const unsigned *__restrict__ outMask,
+                                                     unsigned char *__restrict__ zd) {
+    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= words) return;
+    const unsigned m = qses_find(b.word_off, b.n_mol, q);
+    const QMol &mol = b.mols[m];
+    edt_z_word(mol.g, q - __ldg(b.word_off + m), outMask + mol.mask_off, zd + mol.code_off);
+}
+
 template <int TX, int TY>
 __global__ void __launch_bounds__(kEdtNT) k_edt(QGrid g, const unsigned *__restrict__ inMask,
                                                 const unsigned *__restrict__ outMask,
-                                                unsigned char *__restrict__ codes, unsigned *__restrict__ signMask) {
-    edt_tile<TX, TY>(g, blockIdx.x, blockIdx.y, blockIdx.z, inMask, outMask, codes, signMask);
+                                                unsigned char *__restrict__ codes, unsigned *__restrict__ signMask,
+                                                const unsigned char *__restrict__ zd) {
+    edt_tile<TX, TY>(g, blockIdx.x, blockIdx.y, blockIdx.z, inMask, outMask, codes, signMask, zd);
 }
 
 // ------------------------------------------------------------ batched field
@@ -406,13 +486,14 @@ __global__ void __launch_bounds__(kSasNT) k_sas_batch(QBatch b, const float4 *__
 __global__ void __launch_bounds__(kEdtNT) k_edt_batch(QBatch b, const unsigned *__restrict__ inMask,
                                                       const unsigned *__restrict__ outMask,
                                                       unsigned char *__restrict__ codes,
-                                                      unsigned *__restrict__ signMask, unsigned *counter) {
+                                                      unsigned *__restrict__ signMask, unsigned *counter,
+                                                      const unsigned char *__restrict__ zd) {
     unsigned m;
     int w, jb, ib;
     while (next_tile(b, counter, m, w, jb, ib)) {
         const QMol mol = b.mols[m];
         edt_tile<8, 8>(mol.g, w, jb, ib, inMask + mol.mask_off, outMask + mol.mask_off, codes + mol.code_off,
-                       signMask + mol.mask_off);
+                       signMask + mol.mask_off, zd ? zd + mol.code_off : nullptr);
     }
 }
 
@@ -435,7 +516,7 @@ void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigne
 }
 template <int TX, int TY>
 static void launch_edt_shape(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
-                             unsigned *signMask, cudaStream_t s) {
+                             unsigned *signMask, cudaStream_t s, const unsigned char *zd) {
     constexpr size_t smem = EdtSmem<TX, TY>::bytes;
     static const bool attr = [] {
         return cudaFuncSetAttribute((const void *)k_edt<TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -443,18 +524,23 @@ static void launch_edt_shape(const QGrid &g, const unsigned *inMask, const unsig
     }();
     (void)attr;
     dim3 grid(g.W, (g.G + TY - 1) / TY, (g.G + TX - 1) / TX);
-    k_edt<TX, TY><<<grid, kEdtNT, smem, s>>>(g, inMask, outMask, codes, signMask);
+    k_edt<TX, TY><<<grid, kEdtNT, smem, s>>>(g, inMask, outMask, codes, signMask, zd);
 }
 
 void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
-                unsigned *signMask, cudaStream_t s, int shape) {
+                unsigned *signMask, cudaStream_t s, int shape, unsigned char *zd) {
+    // zd (G G Gp bytes, optional): the z pass once per voxel, then tiles load it
+    if (zd) {
+        const size_t words = (size_t)g.G * g.G * g.W;
+        k_edt_z<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(g, outMask, zd);
+    }
     // shape 0: 8 x 8 rows (37 KB of shared memory), 1: 16 x 8 (48 KB), 2: 16 x 16 (66 KB),
     // 3: 32 x 16 (99 KB)
     switch (shape) {
-        case 3: launch_edt_shape<32, 16>(g, inMask, outMask, codes, signMask, s); break;
-        case 2: launch_edt_shape<16, 16>(g, inMask, outMask, codes, signMask, s); break;
-        case 1: launch_edt_shape<16, 8>(g, inMask, outMask, codes, signMask, s); break;
-        default: launch_edt_shape<8, 8>(g, inMask, outMask, codes, signMask, s); break;
+        case 3: launch_edt_shape<32, 16>(g, inMask, outMask, codes, signMask, s, zd); break;
+        case 2: launch_edt_shape<16, 16>(g, inMask, outMask, codes, signMask, s, zd); break;
+        case 1: launch_edt_shape<16, 8>(g, inMask, outMask, codes, signMask, s, zd); break;
+        default: launch_edt_shape<8, 8>(g, inMask, outMask, codes, signMask, s, zd); break;
     }
 }
 static unsigned persistent_blocks(const void *fn, int threads, unsigned items, size_t smem = 0) {
@@ -471,10 +557,12 @@ void launch_sas_batch(const QBatch &b, unsigned tiles, const float4 *atoms, cons
         b, atoms, cells, inMask, outMask, counter);
 }
 void launch_edt_batch(const QBatch &b, unsigned tiles, const unsigned *inMask, const unsigned *outMask,
-                      unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s) {
+                      unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s, unsigned words,
+                      unsigned char *zd) {
+    if (zd) k_edt_z_batch<<<(words + 255) / 256, 256, 0, s>>>(b, words, outMask, zd);
     constexpr size_t smem = EdtSmem<8, 8>::bytes;
     k_edt_batch<<<persistent_blocks((const void *)k_edt_batch, kEdtNT, tiles, smem), kEdtNT, smem, s>>>(
-        b, inMask, outMask, codes, signMask, counter);
+        b, inMask, outMask, codes, signMask, counter, zd);
 }
 
 }  // namespace qses

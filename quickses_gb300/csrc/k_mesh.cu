@@ -1159,10 +1159,10 @@ cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax,
     void *args[] = {&pos,    &v0,    &nv,          &smax,  (void *)&table, &qcap,         &next_slab,
                     (void *)&home, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
                     &inbox_tail, &err, &spin_cycles, &stats, &idle};
-    // A plain launch: a CTA only waits for slabs taken before its own, by CTAs that were
-    // running when they took them, so no co-residency guarantee is needed, and other kernels
-    // (the side stream's, another lane's) may share the SMs.  P is at most what fits resident.
-    return cudaLaunchKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
+    // A cooperative launch: every CTA resident from the start.  (A plain launch would also be
+    // safe - a CTA only waits for slabs taken before its own, by CTAs that were running when
+    // they took them - but its CTAs can then take the SMs the side stream's kernels wait for.)
+    return cudaLaunchCooperativeKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
 }
 void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes) {
     int max_persist = 0, max_window = 0;

@@ -15,8 +15,10 @@ void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigne
                 cudaStream_t s);
 // shape: refine tile of 8 x 8 (0), 16 x 8 (1), 16 x 16 (2) or 32 x 16 (3) z-rows; the same
 // codes for all.
+// zd (optional, the codes' size): scratch for the z distances, computed once per voxel
+// instead of once per tile halo row.
 void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
-                unsigned *signMask, cudaStream_t s, int shape = 0);
+                unsigned *signMask, cudaStream_t s, int shape = 0, unsigned char *zd = nullptr);
 
 void launch_mc_count(const QGrid &g, const unsigned *sign, uint2 *rowCount, cudaStream_t s);
 void launch_mc_emit(const QGrid &g, const unsigned *sign, const unsigned char *codes, const float *lut,
@@ -86,8 +88,10 @@ constexpr unsigned kGsSlabMaxVerts = 25000;
 void launch_atom_hash_batch(const QBatch &b, const float *xyz, unsigned n, unsigned *key, cudaStream_t s);
 void launch_sas_batch(const QBatch &b, unsigned tiles, const float4 *atoms, const uint2 *cells, unsigned *inMask,
                       unsigned *outMask, unsigned *counter, cudaStream_t s);
+// words: mask words of all molecules; zd (optional, code bytes of all molecules): z distances
 void launch_edt_batch(const QBatch &b, unsigned tiles, const unsigned *inMask, const unsigned *outMask,
-                      unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s);
+                      unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s, unsigned words = 0,
+                      unsigned char *zd = nullptr);
 // Owner rows a marching-cubes warp covers for a grid with Gc emitted cells per axis.
 int mc_rows_per_warp(int Gc);
 void launch_mc_count_batch(const QBatch &b, unsigned units, const unsigned *sign, uint2 *rowCount, cudaStream_t s);

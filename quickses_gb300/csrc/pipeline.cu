@@ -417,7 +417,7 @@ struct FieldSeg {
     float4 *atoms;
     uint2 *cells;
     unsigned *in_mask, *out_mask, *sign_mask;
-    unsigned char *codes;
+    unsigned char *codes, *zd;  // zd: z distances of the refine (scratch)
     float *lut;
     const unsigned char *h_lut;  // pinned; the copy node reads it when the segment runs
     uint2 *rows, *tot;
@@ -445,7 +445,8 @@ static int enqueue_field(qses_context *ctx, const FieldSeg &a, SegOut &o) {
     launch_sas(a.g, a.atoms, a.cells, a.in_mask, a.out_mask, s);
     ctx->launches++;
     ctx->mark("sas");
-    launch_edt(a.g, a.in_mask, a.out_mask, a.codes, a.sign_mask, s, a.edt);
+    launch_edt(a.g, a.in_mask, a.out_mask, a.codes, a.sign_mask, s, a.edt, a.zd);
+    ctx->launches++;
     ctx->launches++;
     ctx->mark("refine");
     launch_mc_count(a.g, a.sign_mask, a.rows, s);
@@ -649,7 +650,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     const int atom_bits = bits_for(ncell ? ncell - 1 : 0);
     size_t tmpA = std::max(radix_sort_tmp_bytes(n, atom_bits), scan_u2_tmp_bytes((unsigned)nrow));
     size_t needA = align256(4ull * n) * 4 + align256(16ull * n) + align256(8 * ncell) + 3 * align256(4 * nmask) +
-                   align256(ncode) + align256(1024) + 2 * align256(8 * nrow) + align256(tmpA) + 4096;
+                   2 * align256(ncode) + align256(1024) + 2 * align256(8 * nrow) + align256(tmpA) + 4096;
     if (ctx->field.reserve(needA) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "field workspace");
     Arena &A = ctx->field;
     FieldSeg a;
@@ -667,6 +668,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     a.out_mask = (unsigned *)A.take(4 * nmask);
     a.sign_mask = (unsigned *)A.take(4 * nmask);
     a.codes = (unsigned char *)A.take(ncode);
+    a.zd = (unsigned char *)A.take(ncode);
     a.lut = (float *)A.take(1024);
     a.rows = (uint2 *)A.take(8 * nrow);
     a.tot = (uint2 *)A.take(64);

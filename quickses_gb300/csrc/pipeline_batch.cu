@@ -72,7 +72,7 @@ struct BatchFieldSeg {
     float4 *atoms;
     uint2 *cells;
     unsigned *in_mask, *out_mask, *sign_mask;
-    unsigned char *codes;
+    unsigned char *codes, *zd;  // zd: z distances of the refine (scratch)
     uint2 *rows, *tot;
     unsigned *counters;
     void *tmp;
@@ -80,8 +80,8 @@ struct BatchFieldSeg {
     unsigned *tri_off, *edge_off;
     unsigned char *h_out;  // pinned: [0, 8) totals, [8, 12) error word
     unsigned long long cell_tot, n_rows;
-    unsigned n, tiles, units;
-    int cell_bits;
+    unsigned n, tiles, units, words;
+    int cell_bits, pad_;
     QBatch b;
 };
 
@@ -105,8 +105,8 @@ static int enqueue_batch_field(qses_context *ctx, const BatchFieldSeg &a, SegOut
     launch_sas_batch(a.b, a.tiles, a.atoms, a.cells, a.in_mask, a.out_mask, a.counters, s);
     ctx->launches++;
     ctx->mark("sas");
-    launch_edt_batch(a.b, a.tiles, a.in_mask, a.out_mask, a.codes, a.sign_mask, a.counters + 1, s);
-    ctx->launches++;
+    launch_edt_batch(a.b, a.tiles, a.in_mask, a.out_mask, a.codes, a.sign_mask, a.counters + 1, s, a.words, a.zd);
+    ctx->launches += 2;
     ctx->mark("refine");
     // marching-cubes counts, one scan over all rows, per-molecule offsets
     launch_mc_count_batch(a.b, a.units, a.sign_mask, a.rows, s);
@@ -296,7 +296,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     // ---- per-molecule layout on the host
     const unsigned nm = count;
     std::vector<QMol> mols(nm);
-    std::vector<unsigned> tile_off(nm + 1), atom_off(nm + 1), row_off(nm + 1), unit_off(nm + 1);
+    std::vector<unsigned> tile_off(nm + 1), atom_off(nm + 1), row_off(nm + 1), unit_off(nm + 1), word_off(nm + 1);
     unsigned long long mask_tot = 0, code_tot = 0, cell_tot = 0, tiles = 0, rows = 0, atoms_tot = 0, units = 0;
     for (unsigned m = 0; m < nm; m++) {
         const QGrid &g = items[m].g;
@@ -313,6 +313,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         atom_off[m] = (unsigned)atoms_tot;
         row_off[m] = (unsigned)rows;
         unit_off[m] = (unsigned)units;
+        word_off[m] = (unsigned)mask_tot;
         mask_tot += (unsigned long long)g.G * g.G * g.W;
         code_tot += (unsigned long long)g.G * g.G * g.Gp;
         cell_tot += (unsigned long long)g.gnb * g.gnb * g.gnb;
@@ -327,12 +328,14 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     atom_off[nm] = (unsigned)atoms_tot;
     row_off[nm] = (unsigned)rows;
     unit_off[nm] = (unsigned)units;
-    if (tiles >= (1ull << 31) || rows >= (1ull << 31) || cell_tot >= (1ull << 31) || atoms_tot >= (1ull << 30))
+    word_off[nm] = (unsigned)mask_tot;
+    if (tiles >= (1ull << 31) || rows >= (1ull << 31) || cell_tot >= (1ull << 31) || atoms_tot >= (1ull << 30) ||
+        mask_tot >= (1ull << 32))
         return ctx->fail(QSES_ERR_UNSUPPORTED, "batch too large for 32-bit item indices; split it");
     const unsigned N = (unsigned)atoms_tot;
 
     // ---- pinned staging: descriptor block then atoms, one copy each
-    const size_t desc_bytes = a256(sizeof(QMol) * nm) + 8 * a256(4ull * (nm + 1)) + a256(1024ull * nm);
+    const size_t desc_bytes = a256(sizeof(QMol) * nm) + 9 * a256(4ull * (nm + 1)) + a256(1024ull * nm);
     const size_t atom_bytes = 16ull * N;
     if (stage_reserve(ctx, desc_bytes + atom_bytes + 256) != QSES_OK)
         return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned batch staging");
@@ -348,6 +351,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     hput(atom_off.data(), 4ull * (nm + 1));
     hput(row_off.data(), 4ull * (nm + 1));
     hput(unit_off.data(), 4ull * (nm + 1));
+    hput(word_off.data(), 4ull * (nm + 1));
     hput(nullptr, 4ull * (nm + 1));  // tri_off   (device-filled)
     hput(nullptr, 4ull * (nm + 1));  // edge_off  (device-filled)
     hput(nullptr, 4ull * (nm + 1));  // vtx_off   (device-filled)
@@ -368,7 +372,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     const int cell_bits = bits_for(cell_tot ? cell_tot - 1 : 0);
     const size_t tmpA = std::max(radix_sort_tmp_bytes(N, cell_bits), scan_u2_tmp_bytes((unsigned)rows));
     const size_t needA = desc_bytes + a256(16ull * N) + 4 * a256(4ull * N) + a256(16ull * N) + a256(8 * cell_tot) +
-                         3 * a256(4 * mask_tot) + a256(code_tot) + a256(8 * rows) + 2 * a256(64) + a256(tmpA) + 8192;
+                         3 * a256(4 * mask_tot) + 2 * a256(code_tot) + a256(8 * rows) + 2 * a256(64) + a256(tmpA) + 8192;
     if (ctx->field.reserve(needA) != QSES_OK) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "batch field workspace");
     Arena &A = ctx->field;
     BatchFieldSeg a;
@@ -395,6 +399,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         b.atom_off = (const unsigned *)at(ob);
         b.row_off = (const unsigned *)at(ob);
         b.mc_unit_off = (const unsigned *)at(ob);
+        b.word_off = (const unsigned *)at(ob);
         b.tri_off = (const unsigned *)at(ob);
         d_edge_off = (unsigned *)at(ob);
         b.vtx_off = (const unsigned *)at(ob);
@@ -414,6 +419,8 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     a.out_mask = (unsigned *)A.take(4 * mask_tot);
     a.sign_mask = (unsigned *)A.take(4 * mask_tot);
     a.codes = (unsigned char *)A.take(code_tot);
+    a.zd = (unsigned char *)A.take(code_tot);
+    a.words = (unsigned)mask_tot;
     a.rows = (uint2 *)A.take(8 * rows);
     a.tot = (uint2 *)A.take(64);
     a.counters = (unsigned *)A.take(64);

@@ -55,6 +55,7 @@ struct QBatch {
     const unsigned *atom_off;
     const unsigned *row_off;
     const unsigned *mc_unit_off; // marching-cubes warp units (32 / lanes rows each)
+    const unsigned *word_off;  // 32-bit mask words (G G W) per molecule
     const unsigned *tri_off;   // pre-filter triangles (valid after the row scan)
     const unsigned *vtx_off;   // welded vertices (valid after the weld)
     const float *lut;          // 256 field values per molecule

@@ -43,7 +43,8 @@ struct Job {
 // workspace), from its grid alone; used only for admission.
 unsigned long long estimate_bytes(const QGrid &g, unsigned n) {
     const double G = g.G;
-    const double field = G * G * (double)g.Gp + 3.0 * G * G * g.W * 4.0 + 8.0 * (double)g.gnb * g.gnb * g.gnb +
+    // codes and the refine's z distances (one byte each per padded voxel), three masks, cells
+    const double field = 2.0 * G * G * (double)g.Gp + 3.0 * G * G * g.W * 4.0 + 8.0 * (double)g.gnb * g.gnb * g.gnb +
                          48.0 * n + 8.0 * (g.Gc + 1.0) * (g.Gc + 1.0);
     const double edges = 12.0 * G * G;  // active edges of a globular surface, generous
     const double mesh = edges * 220.0;  // every mesh array per edge (keys, slots, CSR, positions)
