@@ -181,8 +181,9 @@ QSES_API int qses_set_field_shape(qses_context *ctx, int shape);
  * aimed at (>= 256 vertices), cache_flags bit 0 = prefetch successors' neighbour lists into
  * L1 instead of L2, bit 1 = neighbour positions through L1, bit 2 = keep the positions in
  * persisting L2 lines during the pass (a window on the context's stream, cleared after it),
- * bit 3 = each slab's own positions in shared memory (slabs of at most 8192 vertices);
- * wave_vertices = most vertices per slab-kernel launch (0 = the whole mesh in one launch;
+ * bit 3 = each slab's own positions in shared memory (slabs of at most 8192 vertices),
+ * bit 4 = two vertex updates per worker warp (16 lanes each), bit 5 = four (8 lanes each;
+ * not with bit 4); wave_vertices = most vertices per slab-kernel launch (0 = the whole mesh in one launch;
  * otherwise sequential waves); threads = 0 returns to the tuned/default shape.
  * Every shape gives the same mesh. */
 QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned target, unsigned cache_flags,

@@ -155,7 +155,10 @@ class Context:
 
     def set_smoothing_shape(self, threads=0, target=16384, cache_flags=0, wave_vertices=0):
         """Fix the smoothing launch shape (threads 512/1024, slab target, cache flags, most
-        vertices per slab-kernel wave); threads 0 = tuned/default."""
+        vertices per slab-kernel wave); threads 0 = tuned/default.  cache_flags: bit 0 L1
+        prefetch of successors' lists, bit 1 positions through L1, bit 2 persisting-L2
+        window, bit 3 slab positions in shared memory, bit 4 / bit 5 two / four vertex
+        updates per worker warp."""
         self._check(self._lib.qses_set_smoothing_shape(self._h, int(threads), int(target), int(cache_flags),
                                                        int(wave_vertices)), "qses_set_smoothing_shape")
 

@@ -524,7 +524,7 @@ QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned t
         ctx->gs_force = qses::GsShape{0, 0, 0, 0};
         return QSES_OK;
     }
-    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 15 ||
+    if ((threads != 512 && threads != 1024) || target < 256 || !qses::gs_flags_valid(cache_flags) ||
         (wave_vertices != 0 && wave_vertices < target))
         return QSES_ERR_INVALID_ARG;
     ctx->gs_force = qses::GsShape{threads, target, cache_flags, wave_vertices};
@@ -532,7 +532,8 @@ QSES_API int qses_set_smoothing_shape(qses_context *ctx, int threads, unsigned t
 }
 
 QSES_API int qses_set_default_smoothing_shape(int batch, int threads, unsigned target, unsigned cache_flags) {
-    if ((threads != 512 && threads != 1024) || target < 256 || cache_flags > 15 || (cache_flags & qses::kGsPersistL2))
+    if ((threads != 512 && threads != 1024) || target < 256 || !qses::gs_flags_valid(cache_flags) ||
+        (cache_flags & qses::kGsPersistL2))
         return QSES_ERR_INVALID_ARG;
     qses::gs_shape_record_all(batch != 0, qses::GsShape{threads, target, cache_flags, 0});
     return QSES_OK;
@@ -551,8 +552,8 @@ QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_f
     int rc = check_params(ctx, p);
     if (rc) return rc;
     cudaSetDevice(ctx->device);
-    qses::GsShape cand[64];
-    const int nc = qses::gs_shape_candidates(cand, 64);
+    qses::GsShape cand[128];
+    const int nc = qses::gs_shape_candidates(cand, 128);
     qses::GsShape best = cand[0];
     float best_ms = -1.0f;
     const bool prof = ctx->profiling;
@@ -633,8 +634,8 @@ QSES_API int qses_autotune(qses_context *ctx, const qses_params *p, const qses_f
 QSES_API int qses_autotune_batch(qses_context *ctx, const qses_request *reqs, unsigned count, int repeats,
                                  int *threads_out, unsigned *target_out, unsigned *flags_out, float *ms_out) {
     if (!ctx || (count && !reqs)) return QSES_ERR_INVALID_ARG;
-    qses::GsShape cand[64];
-    const int nc = qses::gs_shape_candidates(cand, 64);
+    qses::GsShape cand[128];
+    const int nc = qses::gs_shape_candidates(cand, 128);
     qses::GsShape best = cand[0];
     double best_s = -1.0;
     unsigned long long nv = 0;

@@ -9,10 +9,9 @@
 //  k_weld_*       unique quantised positions in lexicographic order (CudaSurf.cu:444-457)
 //  k_closest      closest atom per welded vertex (closestAtomPerVertex, Kernels.cu:547-604)
 //  k_tri_*        drop triangles with a repeated index (CudaSurf.cu:820-829)
-//  k_csr_* / k_gs_flow  neighbour lists in triangle order and the in-place Gauss-Seidel Laplacian
-//                 in vertex-id order (SmoothMesh.cpp:45-123), run as a dataflow: a vertex is
-//                 updated once every lower-id neighbour has been, exactly as the sequential
-//                 loop would see them.
+//  k_csr_* / k_gs_setup  neighbour lists in triangle order (getNeighboorsVertices,
+//                 SmoothMesh.cpp:45-123) and the per-vertex dependency counts and slab homes
+//                 of the Gauss-Seidel dataflow (k_smooth.cu)
 #include <cfloat>
 #include <cstdlib>
 #include <cstring>
@@ -626,24 +625,6 @@ __global__ void k_csr_sortfill(const unsigned *__restrict__ tri, unsigned *__res
     start[v] = make_uint2(2u * o, 0u);
 }
 
-__device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
-    int old;
-    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(-v) : "memory");
-    return old;
-}
-
-// Slab-partitioned Gauss-Seidel pass.  Vertex ids are split into P contiguous slabs, one
-// persistent CTA each.  Every dependency edge goes from a lower to a higher id, so a chain
-// of updates crosses each slab boundary at most once: readiness inside a slab is tracked
-// with shared-memory counters and a ring of ready vertices, and only boundary edges go
-// through global memory (an acquire/release counter per vertex and a per-slab inbox).
-// Each vertex is still computed exactly as the sequential loop would.
-constexpr int kGsSlabMaxSmem = 200 * 1024;  // dynamic part: offsets, packed counters, ring: 8 B/vertex
-                                            // (+ 16 B/vertex of positions with kGsSmemPos)
-__host__ __device__ constexpr size_t gs_spos_offset(unsigned smax) {
-    return ((4ull * (smax + 1) + 4ull * ((smax + 1) / 2) + 2ull * smax) + 15) & ~(size_t)15;
-}
-
 // Per vertex: lower-id neighbour entries inside its slab (+1 if any lie in lower slabs),
 // the count of entries in lower slabs, and its home: slab id and the slab's first vertex.
 // Vertices [v0, v1) form the slabs of the table (Q, then Q + 1 bounds in id order).
@@ -674,30 +655,6 @@ __global__ void k_gs_setup(const uint2 *__restrict__ start, const unsigned *__re
     home[v] = make_uint2(lo, a);
 }
 
-// Gauss-Seidel update of one vertex.  Positions are float4 (one 16-byte load each); the
-// first 16 neighbour ids and their positions are all in flight before the in-order sum.
-// Padding lanes add +0.0f, which leaves a sum that started at +0.0f unchanged.
-__device__ __forceinline__ void gs_update4(unsigned v, unsigned e0, unsigned e1, const unsigned *__restrict__ nbr,
-                                           float4 *pos4, unsigned (&id)[16]) {
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for (unsigned base = e0; base < e1; base += 16) {
-        const unsigned m = min(16u, e1 - base);
-#pragma unroll
-        for (unsigned q = 0; q < 16; q++) id[q] = __ldg(nbr + base + (q < m ? q : 0u));
-        float4 pq[16];
-#pragma unroll
-        for (unsigned q = 0; q < 16; q++) pq[q] = __ldcg(pos4 + id[q]);
-#pragma unroll
-        for (unsigned q = 0; q < 16; q++) {
-            sx = __fadd_rn(sx, q < m ? pq[q].x : 0.0f);
-            sy = __fadd_rn(sy, q < m ? pq[q].y : 0.0f);
-            sz = __fadd_rn(sz, q < m ? pq[q].z : 0.0f);
-        }
-    }
-    const float n = (float)(int)(e1 - e0);
-    __stcg(pos4 + v, make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f));
-}
-
 __global__ void k_to_float4(const float *__restrict__ v3, unsigned nv, float4 *__restrict__ v4) {
     unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v < nv) v4[v] = make_float4(v3[3ull * v], v3[3ull * v + 1], v3[3ull * v + 2], 0.0f);
@@ -707,330 +664,6 @@ __global__ void k_from_float4(const float4 *__restrict__ v4, unsigned nv, float 
     if (v < nv) {
         const float4 q = v4[v];
         v3[3ull * v] = q.x; v3[3ull * v + 1] = q.y; v3[3ull * v + 2] = q.z;
-    }
-}
-
-// Two 16-bit readiness counters per shared word; returns the counter value before the
-// decrement.  Counters never go below zero, so no borrow crosses into the other half.
-__device__ __forceinline__ unsigned dec16(unsigned *w, unsigned k) {
-    const unsigned sh = 16u * (k & 1u);
-    return (atomicSub(&w[k >> 1], 1u << sh) >> sh) & 0xffffu;
-}
-
-__device__ __forceinline__ void ring_push16(volatile unsigned short *ring, unsigned *tail, unsigned off) {
-    const unsigned k = atomicAdd(tail, 1u);
-    ring[k] = (unsigned short)off;  // each vertex enters the ring once: no wrap-around
-}
-
-constexpr unsigned kGsOutbox = 1024;  // shared-memory queue of cross-slab releases
-
-__device__ __forceinline__ void prefetch_l2(const void *p) {
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-__device__ __forceinline__ void prefetch_l1(const void *p) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
-// Persistent CTAs take the wave's slabs from a counter, in the table's order (a slab only
-// waits for slabs taken before it, by CTAs that were running when they took them, so every
-// wait ends without a co-residency guarantee).  Per slab,
-// warp 0 takes boundary arrivals from lower slabs, warp 1 sends this slab's cross-slab
-// releases (GPU-scope atomics, off the workers' critical path), the other warps update
-// vertices.  Table: Q, the Q + 1 slab bounds in id order (qcap + 1 slots), then the Q slab ids
-// in the order they are taken.
-template <int kGsT, unsigned kFlags>
-__global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *pos4, unsigned v0, unsigned nv, unsigned smax,
-                                                  const unsigned *__restrict__ table, unsigned qcap,
-                                                  unsigned *next_slab, const uint2 *__restrict__ home,
-                                                  const uint2 *__restrict__ start, const unsigned *__restrict__ nbr,
-                                                  const unsigned short *__restrict__ cnt_local, int *remote,
-                                                  unsigned *inbox, unsigned *inbox_tail, int *err,
-                                                  long long spin_cycles, unsigned long long *stats,
-                                                  unsigned idle_ns_max) {
-    extern __shared__ unsigned s_dyn[];
-    __shared__ unsigned s_head, s_tail, s_done, s_stop, s_ob_head, s_ob_tail, s_slab;
-    __shared__ unsigned s_ob[kGsOutbox];
-    unsigned *st = s_dyn;                                        // len + 1 CSR offsets of the slab
-    unsigned *cnt = s_dyn + (smax + 1);                          // (len + 1) / 2 words: packed counters
-    volatile unsigned short *ring = (volatile unsigned short *)(cnt + (smax + 1) / 2);  // slab offsets
-    // kGsSmemPos: the slab's positions (old until a vertex updates, then new), so neighbours
-    // inside the slab are read from shared memory; others from global memory as before
-    constexpr bool kSP = (kFlags & kGsSmemPos) != 0;
-    float4 *spos = (float4 *)((char *)s_dyn + gs_spos_offset(smax));
-    volatile unsigned *ob = s_ob;
-    const unsigned Q = min(__ldg(table), qcap);
-    const unsigned *bnd = table + 1, *order = table + 2 + qcap;
-    const unsigned lane = threadIdx.x & 31;
-    unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0, cyc_ids = 0, cyc_pos = 0, cyc_fence = 0;
-    if (threadIdx.x == 0) s_stop = 0;
-    for (;;) {
-    if (threadIdx.x == 0) {
-        const unsigned k = atomicAdd(next_slab, 1u);
-        s_slab = (k < Q && !s_stop) ? __ldg(order + k) : 0xffffffffu;
-        s_head = 0; s_tail = 0; s_done = 0; s_ob_head = 0; s_ob_tail = 0;
-    }
-    __syncthreads();
-    const unsigned p = s_slab;
-    if (p >= Q) break;  // uniform per CTA: no slab left (or an error stopped this CTA)
-    const unsigned a = __ldg(bnd + p), b = __ldg(bnd + p + 1), len = b - a;
-    if (a < v0 || b > nv || b <= a || len > smax) {  // uniform: a malformed table entry
-        if (threadIdx.x == 0) raise_error(err, QSES_ERR_INTERNAL);
-        break;
-    }
-    unsigned *box = inbox + (a - v0);                            // boundary arrivals from lower slabs
-    for (unsigned k = threadIdx.x; k < kGsOutbox; k += kGsT) s_ob[k] = 0xffffffffu;
-    for (unsigned k = threadIdx.x; k <= len; k += kGsT) st[k] = start[a + k].x;
-    for (unsigned k = threadIdx.x; k < len; k += kGsT) ring[k] = 0xffffu;
-    if (kSP)
-        for (unsigned k = threadIdx.x; k < len; k += kGsT) spos[k] = __ldcg(pos4 + a + k);
-    for (unsigned k = threadIdx.x; 2 * k < len; k += kGsT) {
-        const unsigned lo = cnt_local[a + 2 * k], hi = 2 * k + 1 < len ? cnt_local[a + 2 * k + 1] : 0u;
-        cnt[k] = lo | (hi << 16);
-    }
-    __syncthreads();
-    for (unsigned k = threadIdx.x; k < len; k += kGsT)
-        if (cnt_local[a + k] == 0) ring_push16(ring, &s_tail, k);
-    __syncthreads();
-
-    if (threadIdx.x < 32) {
-        // Warp 0 only takes boundary arrivals (the last lower-slab dependency of a vertex
-        // finished); it never updates vertices, so arrivals are never stuck behind a chain.
-        if (lane == 0) {
-            unsigned seen = 0, done_seen = 0;
-            long long last = clock64();
-            for (;;) {
-                if (*(volatile unsigned *)&s_done >= len || *(volatile unsigned *)&s_stop) break;
-                const unsigned tail = min(ld_acquire_u32(inbox_tail + p), len);
-                polls++;
-                for (unsigned k = seen; k < tail; k++) {
-                    unsigned u = 0xffffffffu;
-                    for (unsigned it = 0; it < (1u << 20) && u == 0xffffffffu; it++) u = ld_acquire_u32(box + k);
-                    if (u < a || u >= b) {
-                        raise_error(err, u == 0xffffffffu ? QSES_ERR_TIMEOUT : QSES_ERR_INTERNAL);
-                        s_stop = 1;
-                        break;
-                    }
-                    __threadfence_block();
-                    if (dec16(cnt, u - a) == 1u) ring_push16(ring, &s_tail, u - a);
-                }
-                const long long now = clock64();
-                const unsigned d = *(volatile unsigned *)&s_done;
-                if (tail != seen || d != done_seen) last = now;
-                seen = tail;
-                done_seen = d;
-                if (now - last > spin_cycles) {
-                    raise_error(err, QSES_ERR_TIMEOUT);
-                    s_stop = 1;
-                }
-                if (tail == seen) __nanosleep(20);
-            }
-        }
-    } else if (threadIdx.x < 64) {
-        // Warp 1 sends cross-slab releases queued by the workers, up to 32 at a time.  A
-        // worker queues an entry after its position store and a CTA-scope fence; the fence
-        // here plus the GPU-scope acq_rel atomic carry that store to the receiving slab.
-        unsigned head = 0;
-        for (;;) {
-            const unsigned tail = *(volatile unsigned *)&s_ob_tail;
-            const unsigned count = min(tail - head, 32u);
-            if (count == 0) {
-                if (*(volatile unsigned *)&s_stop) break;
-                if (*(volatile unsigned *)&s_done >= len) {
-                    __threadfence_block();
-                    if (*(volatile unsigned *)&s_ob_tail == head) break;  // every worker is done
-                    continue;
-                }
-                __nanosleep(20);
-                continue;
-            }
-            if (lane < count) {
-                volatile unsigned *slot = ob + (head + lane) % kGsOutbox;
-                unsigned u = 0xffffffffu;
-                for (unsigned it = 0; it < (1u << 20) && u == 0xffffffffu; it++) u = *slot;  // reserved slot
-                if (u == 0xffffffffu || u < b || u >= nv) {
-                    raise_error(err, u == 0xffffffffu ? QSES_ERR_TIMEOUT : QSES_ERR_INTERNAL);
-                    s_stop = 1;
-                } else {
-                    *slot = 0xffffffffu;
-                    __threadfence_block();
-                    const uint2 h = __ldg(home + u);  // u's slab and its first vertex (constant)
-                    if (atom_sub_acq_rel(remote + u, 1) == 1) {
-                        // last lower-slab dependency of u: hand u to its slab
-                        const unsigned k = atomicAdd(inbox_tail + h.x, 1u);
-                        if (k < smax && h.x < Q) st_release_u32(inbox + (h.y - v0) + k, u);
-                    }
-                }
-            }
-            head += count;
-            __syncwarp();
-            if (lane == 0) {
-                __threadfence_block();
-                *(volatile unsigned *)&s_ob_head = head;  // slots before head are free again
-            }
-        }
-    } else {
-        // Worker warps: one vertex per warp; lanes fetch neighbours in parallel.  An idle
-        // worker backs off (32 ns doubling up to idle_ns_max, 1 us by default): a hot polling loop of up to
-        // 30 warps would take issue slots and shared-memory bandwidth from the warps on the
-        // critical path.
-        unsigned idle_ns = 0;
-        for (;;) {
-            unsigned v = 0xffffffffu, quit = 0;
-            if (lane == 0) {
-                const unsigned h = *(volatile unsigned *)&s_head, t = *(volatile unsigned *)&s_tail;
-                if (h < t && atomicCAS(&s_head, h, h + 1) == h) {
-                    unsigned off = 0xffffu;
-                    for (unsigned it = 0; it < (1u << 20) && off == 0xffffu; it++) off = ring[h];  // reserved slot
-                    if (off == 0xffffu) {
-                        raise_error(err, QSES_ERR_TIMEOUT);
-                        s_stop = 1;
-                    } else {
-                        v = a + off;
-                    }
-                } else if (h >= t) {
-                    quit = (*(volatile unsigned *)&s_done >= len) || *(volatile unsigned *)&s_stop;
-                }
-            }
-            v = __shfl_sync(0xffffffffu, v, 0);
-            quit = __shfl_sync(0xffffffffu, quit, 0);
-            if (quit) break;
-            if (v == 0xffffffffu) {
-                idle_ns = idle_ns ? min(2 * idle_ns, idle_ns_max) : 32u;
-                __nanosleep(idle_ns);
-                continue;
-            }
-            idle_ns = 0;
-            // Neighbour ids of the vertex this warp continues with, loaded as soon as the
-            // release picked it (the lists are constant, so the early load is always valid).
-            unsigned pre_v = 0xffffffffu, pre_id = 0u;
-            while (v != 0xffffffffu) {  // follow the chain of vertices this warp releases
-                __threadfence_block();
-                const long long c0 = clock64();
-                const unsigned e0 = st[v - a], e1 = st[v - a + 1];
-                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-                unsigned first_id = v;
-                for (unsigned base = e0; base < e1; base += 32) {
-                    const unsigned m = min(32u, e1 - base);
-                    const unsigned id = (base == e0 && pre_v == v) ? pre_id
-                                                                  : (lane < m ? __ldg(nbr + base + lane) : v);
-                    if (base == e0) first_id = id;
-                    long long ca = 0;
-                    if (stats && base == e0) {  // diagnostics: when the ids have arrived (the mov waits for them)
-                        unsigned t;
-                        asm volatile("mov.b32 %0, %1;" : "=r"(t) : "r"(id));
-                        ca = clock64();
-                        cyc_ids += ca - c0 + (t & 0u);
-                    }
-                    // Weak loads either way: the CTA- and GPU-scope acquires above order them.
-                    float4 q;
-                    if (kSP && id - a < len) q = spos[id - a];
-                    else q = (kFlags & kGsL1Positions) ? pos4[id] : __ldcg(pos4 + id);
-                    if (stats && base == e0) {  // ... and their positions
-                        float t;
-                        asm volatile("mov.b32 %0, %1;" : "=f"(t) : "f"(q.x));
-                        cyc_pos += clock64() - ca + (t != t ? 1 : 0);
-                    }
-                    // strictly in neighbour-list order; lanes past m add +0.0f (a sum that
-                    // started at +0.0f is unchanged by it)
-                    const float qx = lane < m ? q.x : 0.0f, qy = lane < m ? q.y : 0.0f, qz = lane < m ? q.z : 0.0f;
-#pragma unroll
-                    for (unsigned k = 0; k < 16; k++) {
-                        sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
-                        sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
-                        sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
-                    }
-                    if (m > 16) {
-#pragma unroll
-                        for (unsigned k = 16; k < 32; k++) {
-                            sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
-                            sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
-                            sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
-                        }
-                    }
-                }
-                const float n = (float)(int)(e1 - e0);
-                if (lane == 0) {
-                    const float4 np = make_float4(__fdiv_rn(sx, n), __fdiv_rn(sy, n), __fdiv_rn(sz, n), 0.0f);
-                    long long cs = 0;
-                    if (stats) {  // diagnostics: the store and its fence (the movs wait for the sums)
-                        float t0, t1, t2;
-                        asm volatile("mov.b32 %0, %3; mov.b32 %1, %4; mov.b32 %2, %5;"
-                                     : "=f"(t0), "=f"(t1), "=f"(t2) : "f"(np.x), "f"(np.y), "f"(np.z));
-                        cs = clock64() + (t0 != t0 || t1 != t1 || t2 != t2 ? 1 : 0);
-                    }
-                    if (kSP) spos[v - a] = np;
-                    __stcg(pos4 + v, np);
-                    // Successors in this slab read the new position after a CTA-scope
-                    // acquire; successors in higher slabs get it through the sender warp.
-                    __threadfence_block();
-                    if (stats) cyc_fence += clock64() - cs;
-                }
-                const long long c1 = clock64();
-                __syncwarp();
-                // Release: one lane per neighbour entry.
-                unsigned next = 0xffffffffu;
-                for (unsigned base = e0; base < e1; base += 32) {
-                    const unsigned m = min(32u, e1 - base);
-                    const unsigned u = lane < m ? (base == e0 ? first_id : __ldg(nbr + base + lane)) : 0u;
-                    // successors at or above nv (the wave's end) belong to a later wave, which
-                    // starts after this one has finished: nothing to release for them
-                    const bool higher = lane < m && u > v && u < nv;
-                    const bool remote_edge = higher && u >= b;
-                    bool ready = false;
-                    if (higher) {
-                        if (!remote_edge) {
-                            // u's list, needed when u runs
-                            if (kFlags & kGsL1Prefetch) prefetch_l1(nbr + st[u - a]);
-                            else prefetch_l2(nbr + st[u - a]);
-                            ready = dec16(cnt, u - a) == 1u;
-                        } else {
-                            const unsigned k = atomicAdd(&s_ob_tail, 1u);
-                            unsigned it = 0;
-                            for (; it < (1u << 22) && k - *(volatile unsigned *)&s_ob_head >= kGsOutbox; it++)
-                                __nanosleep(32);
-                            if (k - *(volatile unsigned *)&s_ob_head >= kGsOutbox) {
-                                raise_error(err, QSES_ERR_TIMEOUT);
-                                s_stop = 1;
-                            } else {
-                                __threadfence_block();  // release: the position store before the entry
-                                ob[k % kGsOutbox] = u;
-                            }
-                        }
-                    }
-                    unsigned mask = __ballot_sync(0xffffffffu, ready);
-                    if (mask && next == 0xffffffffu) {
-                        const unsigned f = __ffs(mask) - 1;
-                        next = __shfl_sync(0xffffffffu, u, f);  // continue with it directly
-                        mask &= ~(1u << f);
-                        const unsigned ne0 = st[next - a], nm = min(32u, st[next - a + 1] - ne0);
-                        pre_id = lane < nm ? __ldg(nbr + ne0 + lane) : next;
-                        pre_v = next;
-                    }
-                    if ((mask >> lane) & 1u) ring_push16(ring, &s_tail, u - a);
-                }
-                __syncwarp();  // queued releases precede the done count the sender checks
-                if (lane == 0) atomicAdd(&s_done, 1u);
-                v = next;
-                const long long c2 = clock64();
-                cyc_update += c1 - c0;
-                cyc_release += c2 - c1;
-                nproc++;
-            }
-        }
-    }
-    __syncthreads();
-    if (stats && threadIdx.x == 0 && s_done < len) atomicAdd(stats + 1, 1ull);  // unfinished slabs
-    }  // next slab
-    if (stats) {  // diagnostics: polls (max), update cycles, release cycles, vertices
-        if (threadIdx.x == 0) atomicMax(stats, polls);
-        if (lane == 0 && nproc) {
-            atomicAdd(stats + 2, cyc_update);
-            atomicAdd(stats + 3, cyc_release);
-            atomicAdd(stats + 4, nproc);
-            atomicAdd(stats + 5, cyc_ids);
-            atomicAdd(stats + 6, cyc_pos);
-            atomicAdd(stats + 7, cyc_fence);
-        }
     }
 }
 
@@ -1119,82 +752,10 @@ void launch_gs_setup(const uint2 *start, const unsigned *nbr, unsigned v0, unsig
                      unsigned short *cnt_local, int *remote, uint2 *home, cudaStream_t s) {
     k_gs_setup<<<nblk(v1 - v0, 256), 256, 0, s>>>(start, nbr, v0, v1, table, cnt_local, remote, home);
 }
-size_t gs_slab_smem(unsigned S, unsigned flags) {
-    return (flags & kGsSmemPos) ? gs_spos_offset(S) + 16ull * S + 16 : 4ull * (S + 1) + 4ull * ((S + 1) / 2) + 2ull * S + 16;
-}
 void launch_to_float4(const float *v3, unsigned nv, float4 *v4, cudaStream_t s) {
     k_to_float4<<<nblk(nv, 256), 256, 0, s>>>(v3, nv, v4);
 }
 void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s) {
     k_from_float4<<<nblk(nv, 256), 256, 0, s>>>(v4, nv, v3);
 }
-static const void *gs_flow_fn(int threads, unsigned flags) {
-    static const void *fn[2][8] = {
-        {(const void *)k_gs_flow<512, 0>, (const void *)k_gs_flow<512, 1>, (const void *)k_gs_flow<512, 2>,
-         (const void *)k_gs_flow<512, 3>, (const void *)k_gs_flow<512, 8>, (const void *)k_gs_flow<512, 9>,
-         (const void *)k_gs_flow<512, 10>, (const void *)k_gs_flow<512, 11>},
-        {(const void *)k_gs_flow<1024, 0>, (const void *)k_gs_flow<1024, 1>, (const void *)k_gs_flow<1024, 2>,
-         (const void *)k_gs_flow<1024, 3>, (const void *)k_gs_flow<1024, 8>, (const void *)k_gs_flow<1024, 9>,
-         (const void *)k_gs_flow<1024, 10>, (const void *)k_gs_flow<1024, 11>}};
-    return fn[threads >= 1024 ? 1 : 0][(flags & 3u) | ((flags & kGsSmemPos) ? 4u : 0u)];
-}
-cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax, const unsigned *table,
-                           unsigned qcap, unsigned *next_slab, const uint2 *home, int P, int threads, unsigned flags,
-                           const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
-                           unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
-                           unsigned long long *stats, cudaStream_t s) {
-    if (smax == 0 || smax > kGsSlabMaxVerts || ((flags & kGsSmemPos) && smax > kGsSmemPosMaxVerts))
-        return cudaErrorInvalidValue;
-    size_t smem = gs_slab_smem(smax, flags);
-    if (smem > (size_t)kGsSlabMaxSmem) return cudaErrorInvalidValue;
-    const void *fn = gs_flow_fn(threads, flags);
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
-    // longest sleep of an idle worker warp (ns); QSES_GS_IDLE_NS overrides it
-    static const unsigned idle_ns_max = [] {
-        const char *e = getenv("QSES_GS_IDLE_NS");
-        const long v = e ? strtol(e, nullptr, 10) : 0;
-        return v >= 32 && v <= 100000 ? (unsigned)v : 1024u;
-    }();
-    unsigned idle = idle_ns_max;
-    void *args[] = {&pos,    &v0,    &nv,          &smax,  (void *)&table, &qcap,         &next_slab,
-                    (void *)&home, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
-                    &inbox_tail, &err, &spin_cycles, &stats, &idle};
-    // A cooperative launch: every CTA resident from the start.  (A plain launch would also be
-    // safe - a CTA only waits for slabs taken before its own, by CTAs that were running when
-    // they took them - but its CTAs can then take the SMs the side stream's kernels wait for.)
-    return cudaLaunchCooperativeKernel(fn, dim3(P), dim3(threads >= 1024 ? 1024 : 512), args, smem, s);
-}
-void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes) {
-    int max_persist = 0, max_window = 0;
-    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, device);
-    cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, device);
-    cudaStreamAttrValue attr;
-    memset(&attr, 0, sizeof(attr));
-    if (bytes > 0 && max_persist > 0 && max_window > 0) {
-        const size_t window = bytes < (size_t)max_window ? bytes : (size_t)max_window;
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)max_persist);
-        attr.accessPolicyWindow.base_ptr = const_cast<void *>(p);
-        attr.accessPolicyWindow.num_bytes = window;
-        attr.accessPolicyWindow.hitRatio = window <= (size_t)max_persist ? 1.0f : (float)max_persist / (float)window;
-        attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-        attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-        cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &attr);
-    } else {
-        attr.accessPolicyWindow.num_bytes = 0;
-        cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &attr);
-        cudaCtxResetPersistingL2Cache();
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
-    }
-    cudaGetLastError();  // the window is a hint: a refusal leaves the results unchanged
-}
-
-int gs_slab_max_blocks(int device, unsigned S, int threads, unsigned flags) {
-    const void *fn = gs_flow_fn(threads, flags);
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSlabMaxSmem);
-    int per_sm = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads >= 1024 ? 1024 : 512, gs_slab_smem(S, flags));
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    return per_sm * sms;
-}
-
 }  // namespace qses

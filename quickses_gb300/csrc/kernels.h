@@ -61,7 +61,7 @@ int gs_slab_max_blocks(int device, unsigned S, int threads, unsigned flags);
 struct GsShape {
     int threads = 512;
     unsigned target = 16384;
-    unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions | kGsPersistL2
+    unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions | kGsPersistL2 | kGsSmemPos | kGsPair / kGsQuad
     unsigned wave = 0;   // most vertices per slab-kernel launch (0: all that fit on the GPU)
 };
 // Cache policies of the smoothing kernel (same results, different memory paths):
@@ -70,6 +70,11 @@ constexpr unsigned kGsL1Positions = 2;  // neighbour positions through L1 (defau
 constexpr unsigned kGsPersistL2 = 4;    // host side: keep the positions in persisting L2 lines
 constexpr unsigned kGsSmemPos = 8;      // the slab's own positions in shared memory (slabs <= 8192)
 constexpr unsigned kGsSmemPosMaxVerts = 8192;
+// Lanes per vertex update (same results): 32 by default; 16 with kGsPair (two ready vertices
+// per worker warp), 8 with kGsQuad (four).
+constexpr unsigned kGsPair = 16;
+constexpr unsigned kGsQuad = 32;
+inline bool gs_flags_valid(unsigned f) { return f < 64 && (f & (kGsPair | kGsQuad)) != (kGsPair | kGsQuad); }
 // Sets (bytes > 0) or clears the stream's L2 persistence window over [p, p + bytes); the
 // set-aside is this process's context limit, restored when the window is cleared.
 void gs_l2_window(int device, cudaStream_t s, const void *p, size_t bytes);

@@ -169,11 +169,18 @@ int gs_shape_candidates(GsShape *out, int max) {
     static const unsigned flags[] = {0,          kGsL1Positions,          kGsL1Prefetch,          kGsL1Prefetch | kGsL1Positions,
                                      kGsSmemPos, kGsSmemPos | kGsL1Positions, kGsSmemPos | kGsL1Prefetch,
                                      kGsSmemPos | kGsL1Prefetch | kGsL1Positions};
+    // two vertices per worker warp with the two policies the one-vertex warps are tuned to:
+    // positions through L1, with or without the slab's own in shared memory (four vertices
+    // per warp, kGsQuad, measured slower than two on single molecules and batches alike)
+    static const unsigned group_flags[] = {kGsPair | kGsL1Positions, kGsPair | kGsSmemPos | kGsL1Positions};
     int k = 0;
     for (int t : {512, 1024})
-        for (unsigned tg : targets)
+        for (unsigned tg : targets) {
             for (unsigned f : flags)
                 if (k < max) out[k++] = GsShape{t, tg, f};
+            for (unsigned f : group_flags)
+                if (k < max) out[k++] = GsShape{t, tg, f};
+        }
     return k;
 }
 

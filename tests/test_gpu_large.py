@@ -67,7 +67,9 @@ def test_smoothing_at_scale_exact(big):
 @pytest.mark.parametrize("threads,target,flags,wave", [(1024, 16384, 0, 0), (1024, 4096, 3, 0), (512, 25000, 2, 0),
                                                        (1024, 16384, 4, 0), (1024, 16384, 6, 0),
                                                        (1024, 16384, 0, 1000000), (512, 8192, 2, 600000),
-                                                       (1024, 8192, 10, 0), (512, 4096, 8, 0), (1024, 8192, 11, 600000)])
+                                                       (1024, 8192, 10, 0), (512, 4096, 8, 0), (1024, 8192, 11, 600000),
+                                                       (1024, 25000, 18, 0), (1024, 8192, 26, 0), (1024, 16384, 34, 0),
+                                                       (512, 8192, 42, 600000), (1024, 4096, 17, 1000000)])
 def test_smoothing_shapes_at_scale_exact(big, threads, target, flags, wave):
     """~150 slabs, every cache policy, and the mesh split into sequential waves (as meshes
     above 3.8 M vertices are): still the sequential Gauss-Seidel result."""

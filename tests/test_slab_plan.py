@@ -140,3 +140,13 @@ def test_batches_shared_memory_positions(seed):
     nv = int(mol_off[-1])
     info, waves = _plan(nv, mol_off, rng.integers(20, 700, nm), target=25000, flags=11)
     _check(nv, mol_off, info, waves)
+
+
+def test_smoothing_flag_validation():
+    # lane-group bits 4 (two vertices per worker warp) and 5 (four) are exclusive; bits above
+    # 5 do not exist.  Invalid shapes are refused before any state changes.
+    lib = L.lib()
+    for flags in (48, 50, 64, 1 << 20):
+        assert lib.qses_set_default_smoothing_shape(1, 1024, 4096, flags) == L.QSES_ERR_INVALID_ARG
+    assert lib.qses_set_default_smoothing_shape(1, 1024, 4096, 4) == L.QSES_ERR_INVALID_ARG  # persisting L2
+    assert lib.qses_set_default_smoothing_shape(1, 768, 4096, 16) == L.QSES_ERR_INVALID_ARG
