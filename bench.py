@@ -299,9 +299,22 @@ def run_gpu(args):
 
 
 def run_once(args):
-    """One pipeline run through the C-ABI (host atoms in, host mesh out): a short program
-    for profiler captures, with few launches before the kernel of interest."""
+    """One pipeline run through the C-ABI (host atoms in, host mesh out), or one batch call
+    with --form batched / trajectory: a short program for profiler captures, with few
+    launches before the kernel of interest."""
     import quickses_gb300 as q
+    if args.form in ("batched", "trajectory"):
+        # one qses_compute_batch of the batch form's molecule stream
+        reqs = q.molecules.uneven_batch(256) if args.form == "batched" else q.molecules.trajectory(512)
+        with q.Context(0) as ctx:
+            if args.gs_shape:
+                ctx.set_smoothing_shape(*[int(x) for x in args.gs_shape.split(",")])
+            out = ctx.compute_batch(reqs)
+            print(json.dumps({"form": args.form, "molecules": len(reqs),
+                              "vertices": int(sum(len(m.vertices) for m in out)),
+                              "triangles": int(sum(len(m.triangles) for m in out)),
+                              "launches": ctx.last_launch_count()}))
+        return
     wl = q.molecules.WORKLOADS[args.workload]
     xyz, rad, _ = wl.atoms()
     with q.Context(0) as ctx:
