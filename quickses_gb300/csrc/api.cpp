@@ -755,7 +755,7 @@ QSES_API int qses_debug_wait_limit(qses_context *ctx, long long spin_cycles, int
     if (e == cudaSuccess) e = cudaMemcpyAsync(home, home_h, sizeof(home_h), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(pos, pos_h, sizeof(pos_h), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
-        e = qses::launch_gs_slab(pos, 0, 4, 2, table, 2, tails + 2, home, 2, 512, 0, start, nbr, cnt, remote, inbox,
+        e = qses::launch_gs_slab(pos, 0, 4, 2, table, 2, tails + 2, home, 2, 512, 0, 0, start, nbr, cnt, remote, inbox,
                                  tails, err, spin_cycles, nullptr, s);
     int h_err = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s);

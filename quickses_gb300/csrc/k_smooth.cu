@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
                                                   const unsigned short *__restrict__ cnt_local, int *remote,
                                                   unsigned *inbox, unsigned *inbox_tail, int *err,
                                                   long long spin_cycles, unsigned long long *stats,
-                                                  unsigned idle_ns_max) {
+                                                  unsigned idle_ns_max, unsigned hot_warps) {
     extern __shared__ unsigned s_dyn[];
     __shared__ unsigned s_head, s_tail, s_done, s_stop, s_ob_head, s_ob_tail, s_slab;
     __shared__ unsigned s_ob[kGsOutbox];
@@ -81,6 +81,10 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
     const unsigned Q = min(__ldg(table), qcap);
     const unsigned *bnd = table + 1, *order = table + 2 + qcap;
     const unsigned lane = threadIdx.x & 31;
+    // longest sleep of this warp when idle: the first hot_warps worker warps poll the ring
+    // every 64 ns at most, so a vertex pushed there is picked up without waiting for a
+    // warp that backed off to idle_ns_max
+    const unsigned idle_cap = (threadIdx.x >> 5) < 2u + hot_warps ? min(64u, idle_ns_max) : idle_ns_max;
     unsigned long long cyc_update = 0, cyc_release = 0, nproc = 0, polls = 0, cyc_ids = 0, cyc_pos = 0, cyc_fence = 0;
     if (threadIdx.x == 0) s_stop = 0;
     for (;;) {
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
             quit = __shfl_sync(0xffffffffu, quit, 0);
             if (quit) break;
             if (v == 0xffffffffu) {
-                idle_ns = idle_ns ? min(2 * idle_ns, idle_ns_max) : 32u;
+                idle_ns = idle_ns ? min(2 * idle_ns, idle_cap) : 32u;
                 __nanosleep(idle_ns);
                 continue;
             }
@@ -387,7 +391,7 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
             }
             const unsigned busy = __ballot_sync(0xffffffffu, gl == 0 && v != 0xffffffffu);
             if (!busy) {
-                idle_ns = idle_ns ? min(2 * idle_ns, idle_ns_max) : 32u;
+                idle_ns = idle_ns ? min(2 * idle_ns, idle_cap) : 32u;
                 __nanosleep(idle_ns);
                 continue;
             }
@@ -537,7 +541,8 @@ static const void *gs_flow_fn(int threads, unsigned flags) {
 }
 cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax, const unsigned *table,
                            unsigned qcap, unsigned *next_slab, const uint2 *home, int P, int threads, unsigned flags,
-                           const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
+                           unsigned hot_warps, const uint2 *start, const unsigned *nbr,
+                           const unsigned short *cnt_local, int *remote,
                            unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
                            unsigned long long *stats, cudaStream_t s) {
     if (smax == 0 || smax > kGsSlabMaxVerts || ((flags & kGsSmemPos) && smax > kGsSmemPosMaxVerts) ||
@@ -553,10 +558,16 @@ cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax,
         const long v = e ? strtol(e, nullptr, 10) : 0;
         return v >= 32 && v <= 100000 ? (unsigned)v : 1024u;
     }();
-    unsigned idle = idle_ns_max;
+    // worker warps that stay hot; QSES_GS_HOT_WARPS (0-30) overrides the caller's count
+    static const int hot_env = [] {
+        const char *e = getenv("QSES_GS_HOT_WARPS");
+        const long v = e ? strtol(e, nullptr, 10) : -1;
+        return v >= 0 && v <= 30 ? (int)v : -1;
+    }();
+    unsigned idle = idle_ns_max, hot = hot_env >= 0 ? (unsigned)hot_env : hot_warps;
     void *args[] = {&pos,    &v0,    &nv,          &smax,  (void *)&table, &qcap,         &next_slab,
                     (void *)&home, (void *)&start, (void *)&nbr, (void *)&cnt_local, &remote, &inbox,
-                    &inbox_tail, &err, &spin_cycles, &stats, &idle};
+                    &inbox_tail, &err, &spin_cycles, &stats, &idle, &hot};
     // A cooperative launch: every CTA resident from the start.  (A plain launch would also be
     // safe - a CTA only waits for slabs taken before its own, by CTAs that were running when
     // they took them - but its CTAs can then take the SMs the side stream's kernels wait for.)

@@ -51,7 +51,8 @@ void launch_from_float4(const float4 *v4, unsigned nv, float *v3, cudaStream_t s
 // counters).  threads: 512 or 1024 per slab CTA.
 cudaError_t launch_gs_slab(float4 *pos, unsigned v0, unsigned nv, unsigned smax, const unsigned *table,
                            unsigned qcap, unsigned *next_slab, const uint2 *home, int P, int threads, unsigned flags,
-                           const uint2 *start, const unsigned *nbr, const unsigned short *cnt_local, int *remote,
+                           unsigned hot_warps, const uint2 *start, const unsigned *nbr,
+                           const unsigned short *cnt_local, int *remote,
                            unsigned *inbox, unsigned *inbox_tail, int *err, long long spin_cycles,
                            unsigned long long *stats, cudaStream_t s);
 int gs_slab_max_blocks(int device, unsigned S, int threads, unsigned flags);
@@ -63,7 +64,12 @@ struct GsShape {
     unsigned target = 16384;
     unsigned flags = 0;  // kGsL1Prefetch | kGsL1Positions | kGsPersistL2 | kGsSmemPos | kGsPair / kGsQuad
     unsigned wave = 0;   // most vertices per slab-kernel launch (0: all that fit on the GPU)
+    unsigned hot = 0;    // worker warps per CTA whose idle sleeps stay short (same results)
 };
+// Hot worker warps of single-molecule passes: 12 of 30 polling the ready ring every 64 ns
+// at most took the 50 000-atom pass from 10.42-10.44 to 10.27-10.29 ms (0: 15.72-15.74 ms
+// per call, 12: 15.51); all 30 hot was slower (16.0 ms); batches are faster with none.
+constexpr unsigned kGsHotWarpsSingle = 12;
 // Cache policies of the smoothing kernel (same results, different memory paths):
 constexpr unsigned kGsL1Prefetch = 1;   // prefetch a successor's neighbour list into L1, not L2
 constexpr unsigned kGsL1Positions = 2;  // neighbour positions through L1 (default: L2 only)

@@ -405,7 +405,7 @@ int run_smoothing(qses_context *ctx, const GsShape &sh, const GsLaunch &L, int p
             QCHK(cudaMemsetAsync(inbox, 0xff, 4ull * (v1 - v0), s));
             QCHK(cudaMemsetAsync(inbox_tail, 0, 4ull * (L.qcap + 1), s));
             QCHK(launch_gs_slab(pos4, v0, v1, L.smax, tb, L.qcap, inbox_tail + L.qcap, home, L.ctas, sh.threads,
-                                sh.flags, deg, nbr, cnt, remote, inbox, inbox_tail, d_err, 4000000000ll, stats, s));
+                                sh.flags, sh.hot, deg, nbr, cnt, remote, inbox, inbox_tail, d_err, 4000000000ll, stats, s));
             ctx->launches++;
         }
     }
@@ -826,6 +826,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     const bool smoothing = p.smooth_passes > 0 && nv > 0 && T > 0;
     if (smoothing) {
         c.sh = ctx->gs_force.threads ? ctx->gs_force : gs_shape(nv, false);
+        c.sh.hot = kGsHotWarpsSingle;
         ctx->gs_used = c.sh;
         GsPlan plan;
         rc = gs_plan(ctx->device, c.sh, nv, nullptr, nullptr, 1, plan);
