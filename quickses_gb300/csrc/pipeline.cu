@@ -789,7 +789,7 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
         dl.d2h = dl.vb + dl.tb + 2 * dl.ab;
     }
     FinishSeg c;
-    memset(&c, 0, sizeof(c));
+    memset((void *)&c, 0, sizeof(c));  // padding too: the key is compared bytewise
     c.atoms = a.atoms;
     c.cells = a.cells;
     c.sidx = sidx;

@@ -531,7 +531,7 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
         dl.d2h = dl.vb + dl.tb + 2 * dl.ab;
     }
     BatchFinishSeg c;
-    memset(&c, 0, sizeof(c));
+    memset((void *)&c, 0, sizeof(c));  // padding too: the key is compared bytewise
     c.atoms = a.atoms;
     c.cells = a.cells;
     c.sidx = sidx;
