@@ -128,7 +128,8 @@ GsShape gs_shape(unsigned nv, bool batch) {
     const int b = tune_bucket(nv);
     if (g_tuned[batch][b]) return g_tune[batch][b];
     // untuned: the shapes the tuner picks on balls of 1 000 - 50 000 atoms and on batches
-    return batch ? GsShape{1024, 25000, kGsL1Positions, 0} : GsShape{1024, 4096, kGsL1Positions, 0};
+    // (two vertex updates per worker warp: 14.1 -> 13.0 ms on a served batch of 23 M vertices)
+    return batch ? GsShape{1024, 25000, kGsL1Positions | kGsPair, 0} : GsShape{1024, 4096, kGsL1Positions, 0};
 }
 
 void gs_shape_record(unsigned nv, bool batch, GsShape sh) {
