@@ -702,7 +702,7 @@ QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int ma
 QSES_API int qses_debug_slab_plan(unsigned nv, const unsigned *mol_off, const int *depth, unsigned nm, int threads,
                                   unsigned target, unsigned cache_flags, unsigned wave, int pmax, unsigned *launch,
                                   unsigned *table, size_t cap) {
-    if (!launch || (nm > 1 && !mol_off)) return QSES_ERR_INVALID_ARG;
+    if (!launch || (nm > 1 && !mol_off) || !qses::gs_flags_valid(cache_flags)) return QSES_ERR_INVALID_ARG;
     qses::GsPlan pl;
     const int rc =
         qses::gs_plan_for(pmax, qses::GsShape{threads, target, cache_flags, wave}, nv, mol_off, depth, nm, pl);

@@ -150,3 +150,20 @@ def test_smoothing_flag_validation():
         assert lib.qses_set_default_smoothing_shape(1, 1024, 4096, flags) == L.QSES_ERR_INVALID_ARG
     assert lib.qses_set_default_smoothing_shape(1, 1024, 4096, 4) == L.QSES_ERR_INVALID_ARG  # persisting L2
     assert lib.qses_set_default_smoothing_shape(1, 768, 4096, 16) == L.QSES_ERR_INVALID_ARG
+    launch = (ctypes.c_uint * 6)()
+    assert lib.qses_debug_slab_plan(1000, None, None, 1, 1024, 4096, 48, 0, 152, launch, None, 0) == L.QSES_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("flags", [16, 18, 32, 34])
+def test_lane_groups_do_not_change_the_plan(flags):
+    # the lane mode is a property of the kernel, not of the slab split
+    rng = np.random.default_rng(7)
+    sizes = rng.integers(100, 200_000, 40)
+    mol_off = np.concatenate([[0], np.cumsum(sizes)])
+    depth = rng.integers(20, 700, 40)
+    base = _plan(int(mol_off[-1]), mol_off, depth, target=25000, flags=flags & 15)
+    info, waves = _plan(int(mol_off[-1]), mol_off, depth, target=25000, flags=flags)
+    assert {k: info[k] for k in ("ctas", "smax", "qcap", "wsize", "waves")} == \
+        {k: base[0][k] for k in ("ctas", "smax", "qcap", "wsize", "waves")}
+    for (b0, o0), (b1, o1) in zip(base[1], waves):
+        assert np.array_equal(b0, b1) and np.array_equal(o0, o1)
