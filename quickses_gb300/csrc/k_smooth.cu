@@ -9,6 +9,7 @@
 #include "kernels.h"
 
 namespace qses {
+
 __device__ __forceinline__ int atom_sub_acq_rel(int *p, int v) {
     int old;
     asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(-v) : "memory");
