@@ -4,15 +4,20 @@ Workload (default): 50 000 heavy atoms uniform in a ball at 0.05 atoms/A^3 (1.2 
 pair distance, C/N/O/S mix), voxel 0.2 A, probe 1.4 A, 1 Laplacian pass - the multi-slice
 single-molecule configuration.  voxels = G^3 of the reference's grid sizing.
 
-* value     G^3 / device time per step, atoms already in HBM (qses_compute_device)
-* e2e       same metric through the C-ABI with host buffers (qses_compute: atom upload,
-            full pipeline, mesh download into library-owned pinned buffers)
-* roofline  dominant stage: algorithmic bytes / its CUDA-event time vs measured HBM peak
-* cpu_baseline  the CPU oracle (all host threads) on the same molecule: the whole pipeline
+* value          G^3 / device time per step, atoms already in HBM (qses_compute_device)
+* e2e            same metric through the C-ABI with host buffers (qses_compute: atom upload,
+                 full pipeline, mesh download into library-owned pinned buffers)
+* roofline       dominant stage: algorithmic bytes / its CUDA-event time vs measured HBM peak
+* other_configs  the 1 000-atom ball (0.5 A) and the 1 M-atom shell (0.5 A, no smoothing):
+                 device and end-to-end times
+* ref_cuda       the reference's own CUDA build (API_computeSES) on the same molecules and
+                 GPU, wall clock, in a child process; ratio = its time / our end-to-end time
+* cpu_baseline   the CPU job of one step on the host cores: the FP64 oracle (field, marching
+                 cubes, weld, closest atom) + the reference's own SmoothMesh.cpp
 
-`--impl reference` times the reference path's CPU implementation instead: QuickSES has no
-CPU field code, so this is the CPU oracle port (C++/OpenMP restatement) on the same
-workload, the whole pipeline per step.
+`--impl reference` times that CPU job per step instead (QuickSES's only CPU code on the path
+is its smoothing; the rest is the oracle, its CPU restatement).  Its inputs come from the
+oracle's generator, so that arm never loads the product library.
 """
 import argparse
 import atexit
@@ -23,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -55,14 +61,14 @@ class ClockSampler:
 
     def __init__(self, device=0, interval_ms=100):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        fd, self.path = tempfile.mkstemp(prefix="qses_clocks_", suffix=".csv")
+        os.close(fd)
         self.device = device
         self.interval_ms = interval_ms
         self.t0 = self.t1 = None
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=timestamp,clocks.sm,clocks.max.sm,power.draw,"
@@ -79,6 +85,10 @@ class ClockSampler:
     def _kill(self):
         if self.proc and self.proc.poll() is None:
             self.proc.terminate()
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
 
     def mark(self):
         self.t0 = datetime.datetime.now()
@@ -138,7 +148,8 @@ def aggregate(world, units_per_rank, ms_max, e2e_ms_max):
 
 
 def algorithmic_bytes(stage, g, n_atoms, T, nv, NE, passes):
-    """Compulsory HBM bytes of one launch of each stage (roofline)."""
+    """Compulsory HBM bytes of one launch of each stage: what the stage must read and write
+    at least once (bit masks, codes, triangles, edge keys, positions, neighbour lists)."""
     G3 = float(g.G) ** 3
     nrow = float(g.Gc + 1) ** 2
     if stage == "sas":
@@ -266,8 +277,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded ball, 0.05 atoms/A^3, 1.2 A min distance, C/N/O/S mix)",
-        "config": {"workload": "%s: %d atoms, voxel %.2f A, probe 1.4 A, %d smoothing pass, grid %d^3"
-                               % (wl.name, n, wl.voxel, wl.smooth, gi.G),
+        "config": {"workload": workload_desc(wl, n, gi.G),
                    "grid_dim": gi.G, "voxels": voxels, "atoms": n, "mesh_vertices": nv, "mesh_triangles": nt,
                    "l2": "flushed between timed steps (256 MB write outside the event pair)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
@@ -289,13 +299,113 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "wall_s": t_wall,
     }
+    if rank == 0 and world == 1 and not args.no_other_configs:
+        # the other single-molecule workloads, device time and end to end, then the
+        # reference's own CUDA build on the same three molecules
+        result["other_configs"] = {k: time_config(ctx, stream, q.molecules.WORKLOADS[k], flush, args)
+                                   for k in ("ball1k", "shell1m")}
+        result["ref_cuda"] = ref_cuda_block(args, {wl.name: (voxels, e2e_ms), **{
+            k: (v["voxels"], v["e2e_ms"]) for k, v in result["other_configs"].items()}})
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(wl, xyz, rad, args.cpu_planes)
+        result["cpu_baseline"] = cpu_baseline(wl, *oracle_atoms(wl), gi.G)
     if world > 1:
         dist.destroy_process_group()
     ctx.close()
     if rank == 0:
         print(json.dumps(result))
+
+
+def time_config(ctx, stream, wl, flush, args):
+    """One more single-molecule workload: device time per call with atoms in HBM (CUDA
+    events on the context stream, L2 flushed between calls) and end-to-end time through
+    qses_compute with host buffers."""
+    import torch
+    import quickses_gb300 as q
+    from quickses_gb300 import _lib as L
+    xyz, rad, _ = wl.atoms()
+    n = len(rad)
+    G = q.grid_info(xyz, rad, wl.voxel).G
+    d_xyz, d_rad = torch.from_numpy(xyz).cuda(), torch.from_numpy(rad).cuda()
+    steps = max(3, min(args.steps, 10))
+    with torch.cuda.stream(stream):
+        if wl.smooth > 0:
+            ctx.autotune(xyz, rad, voxel=wl.voxel, smooth=wl.smooth)
+        for _ in range(3):
+            dm = ctx.compute_device(d_xyz.data_ptr(), d_rad.data_ptr(), n, voxel=wl.voxel, smooth=wl.smooth)
+        times = []
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dm = ctx.compute_device(d_xyz.data_ptr(), d_rad.data_ptr(), n, voxel=wl.voxel, smooth=wl.smooth)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ctx.set_profiling(True)
+        ctx.compute_device(d_xyz.data_ptr(), d_rad.data_ptr(), n, voxel=wl.voxel, smooth=wl.smooth)
+        stages = ctx.stage_times()
+        ctx.set_profiling(False)
+    torch.cuda.synchronize()
+    lib = L.lib()
+    pr = L.Params()
+    lib.qses_params_default(ctypes.byref(pr))
+    pr.voxel, pr.smooth_passes = wl.voxel, wl.smooth
+    mesh, e2e = L.Mesh(), []
+    for it in range(3 + steps):
+        t0 = time.perf_counter()
+        rc = lib.qses_compute(ctx.handle, ctypes.byref(pr), xyz.ctypes.data_as(ctypes.c_void_p),
+                              rad.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n, ctypes.byref(mesh))
+        dt = time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError(lib.qses_last_error(ctx.handle).decode())
+        lib.qses_mesh_release(ctypes.byref(mesh))
+        if it >= 3:
+            e2e.append(dt)
+    del d_xyz, d_rad
+    ms, e2e_ms = float(np.mean(times)), 1e3 * float(np.mean(e2e))
+    return {"workload": workload_desc(wl, n, G), "voxels": float(G) ** 3, "steps": steps,
+            "ms_per_step": ms, "voxels_per_s": float(G) ** 3 / (ms * 1e-3),
+            "e2e_ms": e2e_ms, "e2e_voxels_per_s": float(G) ** 3 / (e2e_ms * 1e-3),
+            "mesh_vertices": dm.n_vertices, "mesh_triangles": dm.n_triangles,
+            "stages_ms": {k: round(v, 4) for k, v in stages}}
+
+
+# Timed calls of the reference's own CUDA build per workload (its 1 M-atom shell runs
+# seconds per call).
+REF_CUDA_CALLS = {"ball1k": 10, "ball50k": 3, "shell1m": 1}
+
+
+def ref_cuda_block(args, ours):
+    """The reference's own CUDA build (oracle/_ref/libQuickSES.so, compiled from its sources
+    for sm_103a by oracle/build.py) on the same molecules and the same GPU, in a child
+    process: wall clock of API_computeSES (host atoms in, host mesh out).  `ours` maps a
+    workload to (voxels, our end-to-end ms through qses_compute); the ratio is ours over
+    the reference's, both end to end."""
+    lib = os.path.join(ROOT, "oracle", "_ref", "libQuickSES.so")
+    if not os.path.exists(lib):
+        return {"unavailable": "the reference's CUDA build (oracle/_ref/libQuickSES.so) was not built: its "
+                               "sources were not at hand"}
+    out = {"path": "API_computeSES of the reference's own CUDA build, wall clock around the call, one molecule "
+                   "per call, same atoms and GPU"}
+    for name, (voxels, e2e_ms) in ours.items():
+        calls = REF_CUDA_CALLS.get(name, 3)
+        try:
+            r = subprocess.run([sys.executable, os.path.join(ROOT, "oracle", "ref_cuda", "run_ref.py"), "bench",
+                                name, str(calls)], capture_output=True, text=True, timeout=args.ref_cuda_timeout)
+            line = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not line:
+                out[name] = {"unavailable": "reference run failed (rc %d): %s" % (
+                    r.returncode, (r.stderr.strip().splitlines() or ["no output"])[-1][:200])}
+                continue
+            d = json.loads(line[-1])
+        except subprocess.TimeoutExpired:
+            out[name] = {"unavailable": "reference run exceeded %d s" % args.ref_cuda_timeout}
+            continue
+        ms = float(np.mean(d["ms"]))
+        out[name] = {"ms_per_call": ms, "voxels_per_s": voxels / (ms * 1e-3), "calls": d["calls"],
+                     "mesh_vertices": d["vertices"], "ours_e2e_ms": e2e_ms,
+                     "ratio_e2e": ms / e2e_ms}
+    return out
 
 
 def run_once(args):
@@ -326,55 +436,115 @@ def run_once(args):
                           "launches": ctx.last_launch_count()}))
 
 
-def cpu_baseline(wl, xyz, rad, planes):
-    """The CPU oracle (FP32 mode, all host threads) on the whole workload: SAS + refine
-    field, marching cubes, weld, closest atom and the sequential Gauss-Seidel pass - the same
-    job as one GPU step.  With `planes` > 0, only the field of that many x-planes (a
-    smaller sample for slow hosts).  voxels/s = voxels covered / time."""
+def workload_desc(wl, n, G):
+    """The workload string both arms print (the same text for the same job)."""
+    return "%s: %d atoms, voxel %.2f A, probe 1.4 A, %d smoothing pass, grid %d^3" % (wl.name, n, wl.voxel,
+                                                                                  wl.smooth, G)
+
+
+def oracle_atoms(wl):
+    """The workload's atoms from the oracle's generator (bit-identical to the library's,
+    tests/test_oracle_synth.py): the CPU legs never load the product library."""
     from oracle import oracle as O
-    g, _ = O.grid(xyz, rad, wl.voxel)
-    cores = os.cpu_count()
-    if planes <= 0 or planes >= g.G:
-        t0 = time.perf_counter()
-        m = O.compute_ses(xyz, rad, wl.voxel, smooth=wl.smooth, fp64=False)
-        dt = time.perf_counter() - t0
-        return {"value": float(g.G) ** 3 / dt, "unit": "voxels/s", "cores": cores, "kind": "port",
-                "sample": "oracle full pipeline on the whole %d^3 grid (field, marching cubes, weld, closest atom, "
-                          "%d Gauss-Seidel pass, %d vertices): %.1f s" % (g.G, wl.smooth, len(m.vertices), dt)}
-    x0 = g.G // 2 - planes // 2
+    if wl.kind == "ball":
+        return O.synth_ball(wl.n_atoms, wl.seed)
+    return O.synth_shell(wl.n_atoms, wl.seed)
+
+
+_REF_SMOOTH = []
+
+
+def _ref_smooth_lib():
+    """The reference's own CPU smoothing (SmoothMesh.cpp, compiled from its sources into
+    oracle/_ref/libqses_ref_host.so), or None when its sources were not at hand."""
+    if not _REF_SMOOTH:
+        lib = None
+        try:
+            from oracle import build as ob
+            path = ob.build_ref()
+            if path:
+                lib = ctypes.CDLL(path)
+                lib.ref_smooth.restype = None
+                lib.ref_smooth.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint,
+                                           ctypes.c_uint]
+        except Exception:  # noqa: BLE001
+            lib = None
+        _REF_SMOOTH.append(lib)
+    return _REF_SMOOTH[0]
+
+
+def cpu_step(wl, xyz, rad):
+    """One CPU pass of the whole job: the FP64 oracle (OpenMP over all host threads) for the
+    field, marching cubes, weld and closest atom, then the reference's own SmoothMesh.cpp
+    (one thread, in place, as the reference runs it after each slice) for the smoothing
+    passes.  Returns (seconds, seconds of the smoothing, description)."""
+    from oracle import oracle as O
+    ref = _ref_smooth_lib() if wl.smooth > 0 else None
     t0 = time.perf_counter()
-    O.field_codes(xyz, rad, g, fp64=False, x0=x0, x1=x0 + planes)
-    dt = time.perf_counter() - t0
-    return {"value": planes * g.G * g.G / dt, "unit": "voxels/s", "cores": cores, "kind": "port",
-            "sample": "oracle SAS+refine on x-planes [%d,%d) of the %d^3 grid (%.1f s); MC/weld/smoothing "
-                      "not included" % (x0, x0 + planes, g.G, dt)}
+    m = O.compute_ses(xyz, rad, wl.voxel, smooth=0 if ref is not None else wl.smooth, fp64=True)
+    t1 = time.perf_counter()
+    if ref is not None:
+        v = np.ascontiguousarray(m.vertices_q, np.float32)
+        t = np.ascontiguousarray(m.triangles, np.int32)
+        ref.ref_smooth(wl.smooth, v.ctypes.data, t.ctypes.data, len(v), len(t))
+    t2 = time.perf_counter()
+    if ref is not None:
+        how = ("FP64 oracle (field, marching cubes, weld, closest atom; %d threads) %.2f s + the reference's "
+               "SmoothMesh.cpp (%d pass, 1 thread, %d vertices) %.2f s" % (os.cpu_count(), t1 - t0, wl.smooth,
+                                                                        len(m.vertices_q), t2 - t1))
+        return t2 - t0, t2 - t1, how
+    how = ("FP64 oracle, whole pipeline including its sequential smoothing (%d threads; the reference's "
+           "SmoothMesh.cpp was not available): %.2f s" % (os.cpu_count(), t1 - t0))
+    return t1 - t0, None, how
+
+
+def cpu_baseline(wl, xyz, rad, G):
+    """The CPU job of one GPU step (cpu_step), once, on the same molecule."""
+    dt, t_smooth, how = cpu_step(wl, xyz, rad)
+    return {"value": float(G) ** 3 / dt, "unit": "voxels/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "the whole %d^3 grid, one molecule: %s" % (G, how),
+            "cpu_smooth_ms": None if t_smooth is None else 1e3 * t_smooth}
+
+
+def _libs_loaded():
+    try:
+        with open("/proc/self/maps") as f:
+            return sorted({ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")})
+    except OSError:
+        return []
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path on the host cores: QuickSES has CPU
+    code only for the smoothing (SmoothMesh.cpp, timed as the reference's own code); the
+    field, marching cubes and weld run in the FP64 oracle, its CPU restatement.  Inputs and
+    grid sizes come from the oracle, so this arm never loads the product library."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    import quickses_gb300 as q
-    wl = q.molecules.WORKLOADS[args.workload]
-    xyz, rad, _ = wl.atoms()
-    times, last = [], None
+    from oracle import oracle as O
+    from quickses_gb300.molecules import WORKLOADS  # plain data; loads no library
+    wl = WORKLOADS[args.workload]
+    xyz, rad = oracle_atoms(wl)
+    g, _ = O.grid(xyz, rad, wl.voxel)
+    times, smooth_times, how = [], [], ""
     for it in range(args.warmup + args.steps):
-        res = cpu_baseline(wl, xyz, rad, args.cpu_planes)
-        last = res
+        dt, t_smooth, how = cpu_step(wl, xyz, rad)
         if it >= args.warmup:
-            times.append(res["value"])
-    v = float(np.mean(times))
-    g = q.grid_info(xyz, rad, wl.voxel)
-    sample = ("CPU oracle port (C++/OpenMP restatement of the reference path; the reference ships no CPU field "
-              "code, and its CPU smoothing is the same sequential Gauss-Seidel loop): " + last["sample"])
+            times.append(dt)
+            if t_smooth is not None:
+                smooth_times.append(t_smooth)
+    sec = float(np.mean(times))
+    v = float(g.G) ** 3 / sec
+    product = [p for p in _libs_loaded() if "libquickses_gb300" in p]
+    assert not product, "the reference arm loaded the product library: %s" % product
     out = {"impl": "reference", "metric": "SES grid voxels/s per molecule", "value": v, "unit": "voxels/s",
-           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": float(g.G) ** 3 / v * 1e3 if args.cpu_planes <= 0 else None,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "%s: %d atoms, voxel %.2f A, %d smoothing pass, grid %d^3"
-                                  % (wl.name, len(rad), wl.voxel, wl.smooth, g.G)},
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": workload_desc(wl, len(rad), g.G)},
            "cpu_baseline": {"value": v, "unit": "voxels/s", "cores": os.cpu_count(), "kind": "port",
-                            "sample": sample},
+                            "sample": "each step the whole %d^3 grid, one molecule: %s" % (g.G, how)},
+           "cpu_smooth_ms": float(np.mean(smooth_times)) * 1e3 if smooth_times else None,
            "e2e": {"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -591,9 +761,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ball50k")
-    ap.add_argument("--cpu-planes", type=int, default=0, help="CPU sample: 0 = the whole pipeline on the whole molecule (default); N > 0 = "
-                         "only the field of N x-planes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the 1 000-atom and 1 M-atom workloads and the reference CUDA build's timings")
+    ap.add_argument("--ref-cuda-timeout", type=int, default=240,
+                    help="seconds per workload for the reference CUDA build's child process")
     ap.add_argument("--form", default="plain", choices=["plain", "batched", "trajectory", "served"],
                     help="plain: one molecule per step (default); batched/trajectory: a molecule stream per step "
                          "through qses_compute_batch; served: Poisson arrivals into qses_server")

@@ -226,7 +226,9 @@ QSES_API int qses_server_create(const qses_server_config *cfg, qses_server **out
 QSES_API int qses_server_submit(qses_server *s, const qses_request *req, unsigned long long *ticket);
 /* Blocks until the ticket's mesh is ready (timeout_s < 0: forever; on QSES_ERR_TIMEOUT the
  * ticket stays valid).  Returns the request's status; *out is then the caller's (release
- * with qses_mesh_release) and the ticket is consumed. */
+ * with qses_mesh_release) and the ticket is consumed.  One waiter per ticket: a wait on a
+ * ticket another thread is already waiting for returns QSES_ERR_INVALID_ARG.  Waits and
+ * submits may come from any threads at the same time. */
 QSES_API int qses_server_wait(qses_server *s, unsigned long long ticket, double timeout_s, qses_mesh *out,
                               qses_ticket_info *info);
 /* [0] batches run, [1] requests served, [2] largest batch, [3] most lanes busy at once,
@@ -304,11 +306,13 @@ QSES_API int qses_graph_stats(qses_context *ctx, unsigned long long *out, int ma
  * `cuda_stream` (NULL = legacy default stream).  Allocates nothing: its working memory is a
  * fixed ~3.5 MB array inside the library, reserved on every GPU that loads the library
  * until the process exits.  Limits: 2 <= n <= 4096 atoms, grid <= 128 voxels and <= 40
- * neighbour cells per axis; larger inputs return QSES_ERR_UNSUPPORTED before any GPU
- * work.  The first call on a device looks up the array's device address (make it before
- * any stream capture).  All calls share the array: the function serialises host threads
- * and waits for its own GPU work before returning; work that overlapped it on the GPU
- * would race on the array. */
+ * neighbour cells per axis, all returning QSES_ERR_UNSUPPORTED.  The atom count is checked
+ * before any GPU work; the grid limits need the atoms' bounds, so they are checked after a
+ * bounds pass on the stream, which the call waits for.  The first call on a device (and the
+ * first after the device's context was replaced, e.g. by cudaDeviceReset) looks up the
+ * array's device address: make it before any stream capture.  All calls share the array:
+ * the function serialises host threads and, on success and on every error, waits for its
+ * own GPU work before returning; work that overlapped it on the GPU would race on it. */
 QSES_API int qses_field_codes_noalloc(const float *d_xyz, const float *d_radii, unsigned n, float voxel,
                                       uint8_t *d_codes, size_t codes_bytes, void *cuda_stream);
 

@@ -1,7 +1,13 @@
-"""Build the CPU oracle (test infrastructure) and, where the reference checkout exists,
-the reference-derived helper library under oracle/_ref/.
+"""Build the CPU oracle (test infrastructure) and, where the reference's sources are at
+hand, the reference-derived helpers under oracle/_ref/.
 
     python oracle/build.py            # oracle/liboracle.so (+ oracle/_ref/ if available)
+
+The reference's sources are taken from, in this order: the `ref` argument, the checkout
+named by $QSES_REFERENCE, or the copy staged into oracle/_ref/src by
+`make -C oracle/ref_cuda stage REF_CHECKOUT=<checkout>` (git-ignored; it travels with the
+working tree to machines without the checkout).  Nothing is built from them when none
+exists.
 
 The oracle is plain C++17 + OpenMP compiled with -ffp-contract=off so that its FP32
 mode is IEEE single precision in the written operation order on both x86-64 and aarch64.
@@ -11,7 +17,15 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DEFAULT = "/root/reference"
+STAGED = os.path.join(HERE, "_ref", "src")
+
+
+def reference_sources(ref=None):
+    """Directory with the reference's sources (see the module docstring), or None."""
+    for d in (ref, os.environ.get("QSES_REFERENCE"), STAGED):
+        if d and os.path.isfile(os.path.join(d, "SmoothMesh.cpp")):
+            return d
+    return None
 
 
 def _run(cmd):
@@ -23,12 +37,12 @@ def _run(cmd):
 
 def build_oracle():
     out = os.path.join(HERE, "liboracle.so")
-    src = os.path.join(HERE, "qses_oracle.cpp")
-    deps = [src, os.path.join(HERE, "qses_oracle.h"), os.path.join(HERE, "mc_table.h")]
+    srcs = [os.path.join(HERE, "qses_oracle.cpp"), os.path.join(HERE, "oracle_synth.cpp")]
+    deps = srcs + [os.path.join(HERE, "qses_oracle.h"), os.path.join(HERE, "mc_table.h")]
     if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
         return out
     _run(["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-          "-o", out, src])
+          "-o", out] + srcs)
     return out
 
 
@@ -36,8 +50,8 @@ def build_ref(ref=None):
     """Compile the reference's host-side code (SmoothMesh.cpp and the __host__ __device__
     helpers of Kernels.cu) from the reference checkout into oracle/_ref/.  Returns the
     library path, or None when the checkout is absent (e.g. on the GPU machine)."""
-    ref = ref or os.environ.get("QSES_REFERENCE", REF_DEFAULT)
-    if not os.path.isdir(ref):
+    ref = reference_sources(ref)
+    if ref is None:
         return None
     outdir = os.path.join(HERE, "_ref")
     os.makedirs(outdir, exist_ok=True)
@@ -62,8 +76,8 @@ def build_ref(ref=None):
 def build_ref_pdb(ref=None):
     """The reference's PDB parser (cpdb/cpdb.cpp) plus a walk shim, into
     oracle/_ref/libqses_ref_pdb.so.  None when the checkout is absent."""
-    ref = ref or os.environ.get("QSES_REFERENCE", REF_DEFAULT)
-    if not os.path.isdir(ref):
+    ref = reference_sources(ref)
+    if ref is None:
         return None
     outdir = os.path.join(HERE, "_ref")
     os.makedirs(outdir, exist_ok=True)
@@ -77,7 +91,20 @@ def build_ref_pdb(ref=None):
     return out
 
 
+def build_ref_cuda(ref=None):
+    """The reference's own CUDA build (oracle/_ref/libQuickSES.so, its Makefile's
+    shared-library recipe for sm_103a) and its field kernels for one slice
+    (oracle/_ref/libref_field.so), by oracle/ref_cuda/Makefile.  Returns the library path,
+    or None without the sources."""
+    ref = reference_sources(ref)
+    if ref is None:
+        return None
+    _run(["make", "-s", "-j2", "-C", os.path.join(HERE, "ref_cuda"), "SRC=" + ref])
+    return os.path.join(HERE, "_ref", "libQuickSES.so")
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_ref())
     print(build_ref_pdb())
+    print(build_ref_cuda())

@@ -79,6 +79,9 @@ def lib():
         L.oracle_point_surface.restype = ctypes.c_double
         L.oracle_smooth_depth.argtypes = [ip, ctypes.c_uint, ctypes.c_uint, ip]
         L.oracle_smooth_depth.restype = ctypes.c_int
+        L.oracle_synth_ball.argtypes = [ctypes.c_uint, ctypes.c_uint64, ctypes.c_float, ctypes.c_float, fp, fp]
+        L.oracle_synth_shell.argtypes = [ctypes.c_uint, ctypes.c_uint64, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_float, fp, fp]
         _lib = L
     return _lib
 
@@ -193,3 +196,23 @@ def smooth_depth(triangles, nv):
     level = np.zeros(nv, np.int32)
     d = lib().oracle_smooth_depth(_ptr(t, ctypes.c_int32), t.shape[0], nv, _ptr(level, ctypes.c_int32))
     return d, level
+
+
+def synth_ball(n, seed=1, density=0.05, min_dist=1.2):
+    """The seeded ball molecule (oracle_synth.cpp): the same atoms as the library's
+    generator, made without loading the library."""
+    xyz = np.zeros((n, 3), np.float32)
+    rad = np.zeros(n, np.float32)
+    if lib().oracle_synth_ball(n, seed, density, min_dist, _ptr(xyz, ctypes.c_float), _ptr(rad, ctypes.c_float)):
+        raise ValueError("oracle_synth_ball failed")
+    return xyz, rad
+
+
+def synth_shell(n, seed=1, r_in=400.0, thickness=30.0, min_dist=1.2):
+    """The seeded shell molecule (oracle_synth.cpp), as synth_ball."""
+    xyz = np.zeros((n, 3), np.float32)
+    rad = np.zeros(n, np.float32)
+    if lib().oracle_synth_shell(n, seed, r_in, thickness, min_dist, _ptr(xyz, ctypes.c_float),
+                                _ptr(rad, ctypes.c_float)):
+        raise ValueError("oracle_synth_shell failed")
+    return xyz, rad

@@ -8,6 +8,8 @@ TEST INFRASTRUCTURE ONLY.  Needs oracle/_ref/libQuickSES.so and oracle/_ref/libr
     python oracle/ref_cuda/run_ref.py fixtures                 # tests/golden/ref_cuda.npz
     python oracle/ref_cuda/run_ref.py stream batched|trajectory|served   # plain path, molecules/s
     python oracle/ref_cuda/run_ref.py smooth ball50k           # SmoothMesh.cpp on the CPU vs ours
+    python oracle/ref_cuda/run_ref.py bench ball50k 3          # the reference alone: wall clock of
+                                                               # API_computeSES (bench.py's ref_cuda)
 
 Timing is wall clock around the reference's API_computeSES (its whole library call:
 upload, slices, host smoothing, concatenation) and around our qses_compute (upload,
@@ -241,7 +243,7 @@ def smooth(names):
     staged sources by oracle/build.py) on our unsmoothed mesh: its time, and whether our
     GPU pass gives the same positions bit for bit."""
     from oracle import build as ob
-    path = ob.build_ref(ref=os.path.join(REF, "src"))
+    path = ob.build_ref()
     L = ctypes.CDLL(path)
     L.ref_smooth.restype = None
     L.ref_smooth.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint]
@@ -285,8 +287,31 @@ def stream(which, limit=None):
                       "ref_molecules_per_s": len(reqs) / total, "ref_voxels_per_s": vox / total}), flush=True)
 
 
+def bench(name, calls):
+    """The reference's API_computeSES alone on one workload: one untimed call, then `calls`
+    timed ones (wall clock around the library call, host atoms in, mesh in its host
+    globals).  Atoms and grid size come from the oracle, so this process loads only the
+    reference's library and the oracle."""
+    from quickses_gb300.molecules import WORKLOADS  # plain data; loads no library
+    wl = WORKLOADS[name]
+    xyz, rad = (O.synth_ball if wl.kind == "ball" else O.synth_shell)(wl.n_atoms, wl.seed)
+    g, _ = O.grid(xyz, rad, wl.voxel)
+    ref = Ref()
+    ref.compute(xyz, rad, wl.voxel, wl.smooth)
+    secs, v, t = [], None, None
+    for _ in range(calls):
+        v, t, _a, dt = ref.compute(xyz, rad, wl.voxel, wl.smooth)
+        secs.append(dt)
+    print(json.dumps({"workload": name, "grid": g.G, "voxels": float(g.G) ** 3, "calls": calls,
+                      "ms": [round(1e3 * x, 3) for x in secs], "vertices": len(v), "triangle_indices": 3 * len(t)}),
+          flush=True)
+
+
 if __name__ == "__main__":
     mode = sys.argv[1]
+    if mode == "bench":
+        bench(sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else 3)
+        sys.exit(0)
     if mode == "stream":
         stream(sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else None)
         sys.exit(0)

@@ -11,8 +11,8 @@ writes two representations:
 * ``oracle/mc_table.h`` - the plain ``int[256][16]`` layout (``-1`` terminated) for the
   CPU oracle, so the oracle does not share the packed decoding with the kernels.
 
-Usage: ``python quickses_gb300/csrc/gen_mc_tables.py [path/to/MarchingCubes.cu]``
-(defaults to the reference checkout at /root/reference).  Both outputs are committed.
+Usage: ``python quickses_gb300/csrc/gen_mc_tables.py path/to/MarchingCubes.cu`` (the file
+from a reference checkout).  Both outputs are committed.
 """
 import os
 import re
@@ -63,7 +63,9 @@ def pack(tri):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/MarchingCubes.cu"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: gen_mc_tables.py path/to/MarchingCubes.cu")
+    ref = sys.argv[1]
     tri, nb = load_reference(ref)
     packed = pack(tri)
     for c in range(256):

@@ -36,6 +36,7 @@ struct Job {
     int status = QSES_OK;
     qses_mesh mesh;
     bool done = false;
+    bool claimed = false;  // a qses_server_wait is waiting for (or has taken) this result
     Clock::time_point t_submit, t_start, t_done;
 };
 
@@ -177,8 +178,9 @@ QSES_API int qses_server_submit(qses_server *s, const qses_request *req, unsigne
     if (req->n > 1) {
         qses_grid_info gi;
         QGrid g;
-        float mn[3] = {100000.0f, 100000.0f, 100000.0f}, mx[3] = {-100000.0f, -100000.0f, -100000.0f}, maxR = 0.0f;
-        for (unsigned a = 0; a < req->n; a++) {
+        // bounds start at atom 0, as the device min/max pass starts from its first atom
+        float mn[3] = {j->xyz[0], j->xyz[1], j->xyz[2]}, mx[3] = {j->xyz[0], j->xyz[1], j->xyz[2]}, maxR = j->r[0];
+        for (unsigned a = 1; a < req->n; a++) {
             for (int q = 0; q < 3; q++) {
                 mn[q] = std::min(mn[q], j->xyz[3ull * a + q]);
                 mx[q] = std::max(mx[q], j->xyz[3ull * a + q]);
@@ -208,11 +210,17 @@ QSES_API int qses_server_wait(qses_server *s, unsigned long long ticket, double 
     std::unique_lock<std::mutex> lock(s->mu);
     auto it = s->jobs.find(ticket);
     if (it == s->jobs.end()) return QSES_ERR_INVALID_ARG;
+    // The Job object itself never moves (the map holds a unique_ptr), but a submit may
+    // rehash the map while this thread waits, so no iterator is kept across the wait.  One
+    // waiter per ticket: a second one is refused instead of racing the first one's erase.
     Job *j = it->second.get();
+    if (j->claimed) return QSES_ERR_INVALID_ARG;
+    j->claimed = true;
     auto ready = [&] { return j->done; };
     if (timeout_s < 0) {
         s->cv_done.wait(lock, ready);
     } else if (!s->cv_done.wait_for(lock, std::chrono::duration<double>(timeout_s), ready)) {
+        j->claimed = false;
         return QSES_ERR_TIMEOUT;  // still queued or running; wait again later
     }
     const int st = j->status;
@@ -222,7 +230,7 @@ QSES_API int qses_server_wait(qses_server *s, unsigned long long ticket, double 
         info->run_s = std::chrono::duration<double>(j->t_done - j->t_start).count();
         info->total_s = std::chrono::duration<double>(j->t_done - j->t_submit).count();
     }
-    s->jobs.erase(it);  // the caller owns the mesh now
+    s->jobs.erase(ticket);  // the caller owns the mesh now
     return st;
 }
 

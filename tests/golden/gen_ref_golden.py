@@ -10,8 +10,8 @@ outputs stored in tests/golden/ref_host.npz:
 * smoothMeshLaplacian (SmoothMesh.cpp:96-123) on a marching-cubes mesh
 * computeClosestAtom per welded vertex (Kernels.cu:547-604)
 
-Usage: python tests/golden/gen_ref_golden.py   (needs /root/reference; run in the build
-container, the GPU machine has no checkout).
+Usage: QSES_REFERENCE=<reference checkout> python tests/golden/gen_ref_golden.py
+(or with the sources staged by `make -C oracle/ref_cuda stage`).
 """
 import ctypes
 import os
@@ -34,7 +34,7 @@ CASES = [("ball", 60, 11, 0.5), ("ball", 40, 12, 0.3)]
 def load_ref():
     path = ob.build_ref()
     if path is None:
-        raise SystemExit("reference checkout not found")
+        raise SystemExit("reference sources not found (set QSES_REFERENCE)")
     L = ctypes.CDLL(path)
     fp, vp = ctypes.c_float, ctypes.c_void_p
     L.ref_compute_in_or_out.restype = ctypes.c_float

@@ -68,3 +68,38 @@ def test_rejected_at_submit():
         assert len(m.triangles) > 0
         e1, _ = srv.wait(srv.submit(xyz[:1], rad[:1], voxel=0.5))  # one atom: empty mesh
         assert len(e1.vertices) == 0
+
+
+def test_waits_while_other_threads_submit(ctx):
+    """Two threads wait for the same ticket while the main thread submits hundreds of small
+    requests (the server's ticket table grows and rehashes under the waiters).  Exactly one
+    waiter gets the mesh, the other is refused with QSES_ERR_INVALID_ARG, and every result
+    equals the request computed alone."""
+    from quickses_gb300 import _lib as L
+    xyz, rad, _ = q.molecules.ball(8000, 4401)
+    small = [q.molecules.ball(int(n), 4500 + k)[:2] for k, n in enumerate(np.linspace(3, 40, 24).astype(int))]
+    with q.Server(lanes=2, memory_budget=6 << 30, max_batch=4) as srv:
+        big = srv.submit(xyz, rad, voxel=0.4, smooth=1)
+        got, refused = [], []
+
+        def waiter():
+            try:
+                got.append(srv.wait(big)[0])
+            except q.QSESError as e:
+                refused.append(e.code)
+
+        th = [threading.Thread(target=waiter) for _ in range(2)]
+        for t in th:
+            t.start()
+        tickets = []
+        for rep in range(12):
+            for k, (s_xyz, s_rad) in enumerate(small):
+                tickets.append((srv.submit(s_xyz, s_rad, voxel=0.5, smooth=1), k))
+        for t in th:
+            t.join()
+        results = [(srv.wait(t)[0], k) for t, k in tickets]
+    assert len(got) == 1 and refused == [L.QSES_ERR_INVALID_ARG]
+    _same(got[0], ctx.compute(xyz, rad, voxel=0.4, smooth=1))
+    alone = [ctx.compute(a, b, voxel=0.5, smooth=1) for a, b in small]
+    for m, k in results:
+        _same(m, alone[k])

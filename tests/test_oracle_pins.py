@@ -84,7 +84,9 @@ def test_smoothing_live_reference_multipass(passes):
 
 def test_mc_tables_match_reference_source():
     """The packed kernel table and the oracle table both equal MarchingCubes.cu:64-343."""
-    src = "/root/reference/MarchingCubes.cu"
+    from oracle import build as ob
+    refdir = ob.reference_sources()
+    src = os.path.join(refdir, "MarchingCubes.cu") if refdir else ""
     root = os.path.dirname(HERE)
     packed = open(os.path.join(root, "quickses_gb300", "csrc", "mc_tables.h")).read()
     words = [int(x, 16) for x in re.findall(r"0x([0-9a-f]{16})ULL", packed)]
