@@ -28,7 +28,9 @@ class _Mesh(ctypes.Structure):
                 ("tri", ctypes.POINTER(ctypes.c_int32)), ("tri_kept", ctypes.POINTER(ctypes.c_int32)),
                 ("atom_sorted", ctypes.POINTER(ctypes.c_int32)),
                 ("atom_input", ctypes.POINTER(ctypes.c_int32)),
-                ("edge_vertex", ctypes.POINTER(ctypes.c_int32))]
+                ("edge_vertex", ctypes.POINTER(ctypes.c_int32)),
+                ("nslices", ctypes.c_uint), ("slice_v", ctypes.POINTER(ctypes.c_uint32)),
+                ("slice_t", ctypes.POINTER(ctypes.c_uint32)), ("slice_tk", ctypes.POINTER(ctypes.c_uint32))]
 
 
 @dataclass
@@ -40,6 +42,9 @@ class Mesh:
     atom_sorted: np.ndarray
     atom_input: np.ndarray
     n_edges: int
+    slice_v: np.ndarray = None   # reference slicing mode: first vertex / triangle / kept
+    slice_t: np.ndarray = None   # triangle of each slice, then the totals
+    slice_tk: np.ndarray = None
 
 
 _lib = None
@@ -67,6 +72,9 @@ def lib():
         L.oracle_compute_ses.argtypes = [fp, fp, ctypes.c_uint, ctypes.c_float, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_int]
         L.oracle_compute_ses.restype = ctypes.POINTER(_Mesh)
+        L.oracle_compute_ses_slices.argtypes = [fp, fp, ctypes.c_uint, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int]
+        L.oracle_compute_ses_slices.restype = ctypes.POINTER(_Mesh)
         L.oracle_mesh_free.argtypes = [ctypes.POINTER(_Mesh)]
         L.oracle_smooth_f32.argtypes = [fp, ctypes.c_uint, ctypes.POINTER(ctypes.c_int32), ctypes.c_uint,
                                         ctypes.c_int]
@@ -147,6 +155,10 @@ def _take(mp):
     out = Mesh(arr(m.v, 3 * m.nv, np.float64, 3), arr(m.vq, 3 * m.nv, np.float64, 3),
                arr(m.tri, 3 * m.nt, np.int32, 3), arr(m.tri_kept, 3 * m.nt_kept, np.int32, 3),
                arr(m.atom_sorted, m.nv, np.int32), arr(m.atom_input, m.nv, np.int32), int(m.ne))
+    if m.slice_v:
+        out.slice_v = arr(m.slice_v, m.nslices + 1, np.int64)
+        out.slice_t = arr(m.slice_t, m.nslices + 1, np.int64)
+        out.slice_tk = arr(m.slice_tk, m.nslices + 1, np.int64)
     lib().oracle_mesh_free(mp)
     return out
 
@@ -162,6 +174,14 @@ def compute_ses(xyz, rad, dx, smooth=1, fp64=False, threads=0):
     xyz, rad = _f(xyz), _f(rad)
     return _take(lib().oracle_compute_ses(_ptr(xyz, ctypes.c_float), _ptr(rad, ctypes.c_float), len(rad),
                                           ctypes.c_float(dx), smooth, int(fp64), threads))
+
+
+def compute_ses_slices(xyz, rad, dx, slice_, smooth=1, fp64=False, threads=0):
+    """The reference's slicing (-s slice_): per-slice meshes concatenated as API_computeSES
+    does; slice_v / slice_t / slice_tk give each slice's first vertex and triangle."""
+    xyz, rad = _f(xyz), _f(rad)
+    return _take(lib().oracle_compute_ses_slices(_ptr(xyz, ctypes.c_float), _ptr(rad, ctypes.c_float), len(rad),
+                                                 ctypes.c_float(dx), int(slice_), smooth, int(fp64), threads))
 
 
 def smooth_f32(vertices, triangles, passes):

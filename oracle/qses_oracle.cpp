@@ -17,6 +17,8 @@
  *   closest atom per vertex .... Kernels.cu:547-604
  *   Laplacian smoothing ........ SmoothMesh.cpp:26-123
  *   concatenation + filter ..... CudaSurf.cu:787-841
+ *   reference slicing mode ..... CudaSurf.cu:629-754 (per-slice boxes, seam cell ranges,
+ *                                the unwritten last triangle, per-slice weld and smoothing)
  */
 #include "qses_oracle.h"
 #include "mc_table.h"
@@ -252,6 +254,7 @@ template <> struct Quant<F32> {
         float t = (-fa) / (fb - fa);                       /* MarchingCubes.cu:731-734 */
         return fmaf(t, pb - pa, pa);
     }
+    static float offset(int o, float dx) { return (float)o * dx; }
 };
 template <> struct Quant<F64> {
     static int64_t q(double v) { return (int64_t)std::llround(v / (double)kWeldTol); }
@@ -260,29 +263,47 @@ template <> struct Quant<F64> {
         double t = (-fa) / (fb - fa);
         return pa + t * (pb - pa);
     }
+    static double offset(int o, float dx) { return (double)o * (double)dx; }
+};
+
+/* One box of the reference's slicing (CudaSurf.cu:629-682): D^3 voxels whose index
+   (i, j, k) is voxel (i, j, k) + off of the grid; cells [clo, chi) per axis are emitted
+   (countVertexPerCell's rules, MarchingCubes.cu:578-604).  Without a box the whole grid is
+   one box: D = G, off = 0, cells [0, Gc). */
+struct BoxView {
+    int D;
+    int off[3];
+    int clo[3], chi[3];
 };
 
 template <class P>
-oracle_mesh *mesh_from_codes(const uint8_t *codes, const oracle_grid *g, const Atoms &A) {
+oracle_mesh *mesh_from_codes(const uint8_t *codes, const oracle_grid *g, const Atoms &A,
+                             const BoxView *bv = nullptr) {
     typedef typename P::T T;
-    const int G = g->G, Gc = g->Gc;
+    BoxView whole = {g->G, {0, 0, 0}, {0, 0, 0}, {g->Gc, g->Gc, g->Gc}};
+    const BoxView &box = bv ? *bv : whole;
+    const int G = box.D;
+    const int lox = box.clo[0], hix = box.chi[0], loy = box.clo[1], hiy = box.chi[1], loz = box.clo[2], hiz = box.chi[2];
+    const int Gc = std::max(hix, std::max(hiy, hiz));
+    const bool shifted = (box.off[0] | box.off[1] | box.off[2]) != 0;
     Lut<P> lut(g);
     auto code = [&](int i, int j, int k) { return codes[((size_t)i * G + j) * G + k]; };
     auto neg = [&](int i, int j, int k) { return lut.v[code(i, j, k)] < (T)0; };
 
     oracle_mesh *m = (oracle_mesh *)calloc(1, sizeof(oracle_mesh));
-    if (Gc <= 0) return m;
+    if (Gc <= 0 || lox >= hix || loy >= hiy || loz >= hiz) return m;
     const int64_t E = Gc + 1;
-    /* Active edges in owner-voxel linear order; voxel (i,j,k) owns its +x, +y, +z edges. */
+    /* Active edges in owner-voxel linear order; voxel (i,j,k) owns its +x, +y, +z edges.
+       An edge counts when an emitted cell has it. */
     std::vector<int64_t> eid;
-    for (int i = 0; i <= Gc; i++)
-        for (int j = 0; j <= Gc; j++)
-            for (int k = 0; k <= Gc; k++) {
+    for (int i = lox; i <= hix; i++)
+        for (int j = loy; j <= hiy; j++)
+            for (int k = loz; k <= hiz; k++) {
                 bool s = neg(i, j, k);
                 int64_t base = ((i * E + j) * E + k) * 3;
-                if (i < Gc && s != neg(i + 1, j, k)) eid.push_back(base + 0);
-                if (j < Gc && s != neg(i, j + 1, k)) eid.push_back(base + 1);
-                if (k < Gc && s != neg(i, j, k + 1)) eid.push_back(base + 2);
+                if (i < hix && s != neg(i + 1, j, k)) eid.push_back(base + 0);
+                if (j < hiy && s != neg(i, j + 1, k)) eid.push_back(base + 1);
+                if (k < hiz && s != neg(i, j, k + 1)) eid.push_back(base + 2);
             }
     const size_t ne = eid.size();
     auto slot_of = [&](int i, int j, int k, int axis) -> int32_t {
@@ -296,9 +317,9 @@ oracle_mesh *mesh_from_codes(const uint8_t *codes, const oracle_grid *g, const A
                                      {0, 0, 1, 0}, {1, 0, 1, 1}, {0, 1, 1, 0}, {0, 0, 1, 1},
                                      {0, 0, 0, 2}, {1, 0, 0, 2}, {1, 1, 0, 2}, {0, 1, 0, 2}};
     std::vector<int32_t> tri;
-    for (int i = 0; i < Gc; i++)
-        for (int j = 0; j < Gc; j++)
-            for (int k = 0; k < Gc; k++) {
+    for (int i = lox; i < hix; i++)
+        for (int j = loy; j < hiy; j++)
+            for (int k = loz; k < hiz; k++) {
                 int ci = 0;
                 for (int c = 0; c < 8; c++)
                     if (neg(i + kCorner[c][0], j + kCorner[c][1], k + kCorner[c][2])) ci |= 1 << c;
@@ -326,6 +347,7 @@ oracle_mesh *mesh_from_codes(const uint8_t *codes, const oracle_grid *g, const A
             T pa = P::vox(ijk[c], g->dx, org[c]);
             T v = pa;
             if (c == axis) v = Quant<P>::interp(pa, P::vox(ijk[c] + 1, g->dx, org[c]), fa, fb);
+            if (shifted) v = v + Quant<P>::offset(box.off[c], g->dx); /* MarchingCubes.cu:841-848 */
             mq[s * 3 + c] = Quant<P>::q(v);
         }
     }
@@ -450,6 +472,172 @@ void finish_mesh(oracle_mesh *m, int smooth, int fp64) {
     m->nt_kept = (unsigned)(kept.size() / 3);
     m->tri_kept = (int32_t *)malloc(sizeof(int32_t) * (kept.size() ? kept.size() : 1));
     if (!kept.empty()) memcpy(m->tri_kept, kept.data(), sizeof(int32_t) * kept.size());
+}
+
+/* ---------------- the reference's slicing (CudaSurf.cu:629-754) ---------------- */
+
+/* Voxel codes of one slice box, as probeIntersection and distanceFieldRefine compute them
+   on a slice (Kernels.cu:394-545, launched by CudaSurf.cu:653-729): box voxels at or past
+   lim on an axis keep the memset value probe (outside); the others are classified at their
+   grid index off + (i, j, k) (sas_class applies the grid's own last layer); a border
+   voxel's refine window is clamped to the box (Kernels.cu:517-523).  Returns the number of
+   border voxels (notEmptyCells, CudaSurf.cu:688-691). */
+template <class P>
+size_t box_codes(const oracle_grid *g, const Atoms &A, int D, const int off[3], const int lim[3], uint8_t *codes) {
+    const int R = g->R;
+    const unsigned N = (unsigned)A.x.size();
+    std::vector<float> tin(N), tsas(N);
+    for (unsigned s = 0; s < N; s++) P::thresholds(A.r[s], g->dx, tin[s], tsas[s]);
+    const size_t D2 = (size_t)D * D;
+    std::vector<uint8_t> cls(D2 * D);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < D; i++)
+        for (int j = 0; j < D; j++)
+            for (int k = 0; k < D; k++) {
+                const bool kept = i >= lim[0] || j >= lim[1] || k >= lim[2];
+                cls[i * D2 + (size_t)j * D + k] =
+                    kept ? 0 : (uint8_t)sas_class<P>(off[0] + i, off[1] + j, off[2] + k, g, A, tin, tsas);
+            }
+    struct Off { int di, dj, dk, n; };
+    std::vector<Off> offs;
+    for (int a = -R; a <= R; a++)
+        for (int b = -R; b <= R; b++)
+            for (int c = -R; c <= R; c++) offs.push_back({a, b, c, a * a + b * b + c * c});
+    std::stable_sort(offs.begin(), offs.end(), [](const Off &p, const Off &q) { return p.n < q.n; });
+    size_t border = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : border)
+    for (int i = 0; i < D; i++)
+        for (int j = 0; j < D; j++)
+            for (int k = 0; k < D; k++) {
+                const uint8_t c = cls[i * D2 + (size_t)j * D + k];
+                uint8_t code = c == 0 ? ORACLE_CODE_OUT : ORACLE_CODE_IN;
+                if (c == 1) {
+                    border++;
+                    code = ORACLE_CODE_NONE;
+                    for (const Off &o : offs) {
+                        const int a = i + o.di, b = j + o.dj, d = k + o.dk;
+                        if (a < 0 || b < 0 || d < 0 || a >= D || b >= D || d >= D) continue;
+                        if (cls[a * D2 + (size_t)b * D + d] == 0) {
+                            code = (uint8_t)o.n;
+                            break;
+                        }
+                    }
+                }
+                codes[i * D2 + (size_t)j * D + k] = code;
+            }
+    return border;
+}
+
+/* Cells of one box axis that countVertexPerCell emits (MarchingCubes.cu:578-604), its
+   int bounds compared with the unsigned cell index as the kernel does: [lo, hi), empty as
+   lo == hi. */
+void box_cells(int D, int R, int off, int &lo, int &hi) {
+    lo = hi = 0;
+    bool any = false;
+    for (int c = 0; c < D; c++) {
+        const unsigned i = (unsigned)c;
+        bool skip = i > (unsigned)(D - 2);
+        if (off != 0 && i < (unsigned)(R - 3)) skip = true;
+        if (off == 0 && i >= (unsigned)(D - R * 2 - 1)) skip = true;
+        if (i >= (unsigned)(D - R - 1)) skip = true;
+        if (!skip) {
+            if (!any) lo = c;
+            any = true;
+            hi = c + 1;
+        }
+    }
+}
+
+/* generateTriangleVerticesSMEM writes indices below totalVerts - 3 only (MarchingCubes.cu:845
+   with CudaSurf.cu:421): a slice's last triangle is never written.  It is dropped here, with
+   every vertex that only it used; the other vertices keep their order. */
+void drop_last_triangle(oracle_mesh *m) {
+    if (m->nt == 0) return;
+    m->nt--;
+    std::vector<char> used(m->nv, 0);
+    for (size_t q = 0; q < (size_t)m->nt * 3; q++) used[m->tri[q]] = 1;
+    std::vector<int32_t> id(m->nv, -1);
+    unsigned nv = 0;
+    for (unsigned v = 0; v < m->nv; v++)
+        if (used[v]) {
+            id[v] = (int32_t)nv;
+            for (int c = 0; c < 3; c++) {
+                m->vq[3 * nv + c] = m->vq[3 * v + c];
+                m->v[3 * nv + c] = m->v[3 * v + c];
+            }
+            m->atom_sorted[nv] = m->atom_sorted[v];
+            m->atom_input[nv] = m->atom_input[v];
+            nv++;
+        }
+    m->nv = nv;
+    for (size_t q = 0; q < (size_t)m->nt * 3; q++) m->tri[q] = id[m->tri[q]];
+    for (unsigned e = 0; e < m->ne; e++) m->edge_vertex[e] = id[m->edge_vertex[e]];
+}
+
+/* computeSlicedSES's slice loop (CudaSurf.cu:629-754) and API_computeSES's concatenation
+   (CudaSurf.cu:796-836): cores of S = min(slice, G) voxels, boxes of D = min(slice + 2R, G)
+   voxels starting R before each core (clamped at 0), x outermost; a slice without border
+   voxels gives no mesh; each slice's mesh is welded and smoothed alone; vertex ids of later
+   slices are offset by the vertices before them. */
+template <class P>
+oracle_mesh *sliced_ses(const float *xyz, const float *rad, unsigned N, const oracle_grid *g, int slice, int smooth,
+                        int fp64) {
+    Atoms A;
+    build_atoms(xyz, rad, N, g, A);
+    const int G = g->G, R = g->R;
+    const int S = std::min(slice, G), D = std::min(slice + 2 * R, G);
+    std::vector<oracle_mesh *> parts;
+    std::vector<uint8_t> codes((size_t)D * D * D);
+    for (int x = 0; x < G; x += S)
+        for (int y = 0; y < G; y += S)
+            for (int z = 0; z < G; z += S) {
+                const int core[3] = {x, y, z};
+                int off[3], lim[3];
+                BoxView bv;
+                bv.D = D;
+                for (int a = 0; a < 3; a++) {
+                    off[a] = std::max(0, core[a] - R);
+                    lim[a] = std::min(D - 1, G - 1 - off[a]);
+                    bv.off[a] = off[a];
+                    box_cells(D, R, off[a], bv.clo[a], bv.chi[a]);
+                }
+                if (box_codes<P>(g, A, D, off, lim, codes.data()) == 0) continue;
+                oracle_mesh *m = mesh_from_codes<P>(codes.data(), g, A, &bv);
+                drop_last_triangle(m);
+                finish_mesh(m, smooth, fp64);
+                parts.push_back(m);
+            }
+    oracle_mesh *out = (oracle_mesh *)calloc(1, sizeof(oracle_mesh));
+    const unsigned ns = (unsigned)parts.size();
+    out->nslices = ns;
+    out->slice_v = (uint32_t *)calloc(ns + 1, sizeof(uint32_t));
+    out->slice_t = (uint32_t *)calloc(ns + 1, sizeof(uint32_t));
+    out->slice_tk = (uint32_t *)calloc(ns + 1, sizeof(uint32_t));
+    for (unsigned q = 0; q < ns; q++) {
+        out->slice_v[q + 1] = out->slice_v[q] + parts[q]->nv;
+        out->slice_t[q + 1] = out->slice_t[q] + parts[q]->nt;
+        out->slice_tk[q + 1] = out->slice_tk[q] + parts[q]->nt_kept;
+    }
+    const unsigned nv = out->slice_v[ns], nt = out->slice_t[ns], ntk = out->slice_tk[ns];
+    out->nv = nv; out->nt = nt; out->nt_kept = ntk;
+    out->v = (double *)malloc(sizeof(double) * 3 * (nv ? nv : 1));
+    out->vq = (double *)malloc(sizeof(double) * 3 * (nv ? nv : 1));
+    out->tri = (int32_t *)malloc(sizeof(int32_t) * 3 * (nt ? nt : 1));
+    out->tri_kept = (int32_t *)malloc(sizeof(int32_t) * 3 * (ntk ? ntk : 1));
+    out->atom_sorted = (int32_t *)malloc(sizeof(int32_t) * (nv ? nv : 1));
+    out->atom_input = (int32_t *)malloc(sizeof(int32_t) * (nv ? nv : 1));
+    for (unsigned q = 0; q < ns; q++) {
+        const oracle_mesh *m = parts[q];
+        const unsigned v0 = out->slice_v[q], t0 = out->slice_t[q], k0 = out->slice_tk[q];
+        memcpy(out->v + 3ull * v0, m->v, sizeof(double) * 3 * m->nv);
+        memcpy(out->vq + 3ull * v0, m->vq, sizeof(double) * 3 * m->nv);
+        memcpy(out->atom_sorted + v0, m->atom_sorted, sizeof(int32_t) * m->nv);
+        memcpy(out->atom_input + v0, m->atom_input, sizeof(int32_t) * m->nv);
+        for (size_t e = 0; e < 3ull * m->nt; e++) out->tri[3ull * t0 + e] = m->tri[e] + (int32_t)v0;
+        for (size_t e = 0; e < 3ull * m->nt_kept; e++) out->tri_kept[3ull * k0 + e] = m->tri_kept[e] + (int32_t)v0;
+        oracle_mesh_free(parts[q]);
+    }
+    return out;
 }
 
 /* ---------------- point-to-triangle distance for Hausdorff ---------------- */
@@ -664,10 +852,22 @@ oracle_mesh *oracle_compute_ses(const float *xyz, const float *rad, unsigned N, 
     return oracle_mesh_from_codes(codes.data(), &g, fp64, xyz, N, smooth, nthreads);
 }
 
+oracle_mesh *oracle_compute_ses_slices(const float *xyz, const float *rad, unsigned N, float dx, int slice,
+                                       int smooth, int fp64, int nthreads) {
+    oracle_grid g;
+    if (slice < 1) return nullptr;
+    if (oracle_grid_setup(xyz, rad, N, dx, &g) != 0) return (oracle_mesh *)calloc(1, sizeof(oracle_mesh));
+    if (3 * g.R * g.R > 252) return nullptr;
+    set_threads(nthreads);
+    return fp64 ? sliced_ses<F64>(xyz, rad, N, &g, slice, smooth, fp64)
+                : sliced_ses<F32>(xyz, rad, N, &g, slice, smooth, fp64);
+}
+
 void oracle_mesh_free(oracle_mesh *m) {
     if (!m) return;
     free(m->v); free(m->vq); free(m->tri); free(m->tri_kept);
     free(m->atom_sorted); free(m->atom_input); free(m->edge_vertex);
+    free(m->slice_v); free(m->slice_t); free(m->slice_tk);
     free(m);
 }
 

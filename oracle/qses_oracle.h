@@ -52,6 +52,10 @@ typedef struct {
     int32_t *atom_sorted; /* nv closest atom, index into the cell-sorted atom array */
     int32_t *atom_input;  /* nv closest atom, caller's input index */
     int32_t *edge_vertex; /* ne: pre-weld edge slot -> welded vertex */
+    unsigned nslices;     /* reference slicing mode: slices with a mesh, in slice order */
+    uint32_t *slice_v;    /* nslices+1: first vertex of each slice (then the total) */
+    uint32_t *slice_t;    /* nslices+1: first triangle (all) of each slice */
+    uint32_t *slice_tk;   /* nslices+1: first kept triangle of each slice */
 } oracle_mesh;
 
 int oracle_grid_setup(const float *xyz, const float *rad, unsigned N, float dx, oracle_grid *g);
@@ -65,6 +69,10 @@ oracle_mesh *oracle_mesh_from_codes(const uint8_t *codes, const oracle_grid *g, 
                                     const float *xyz, unsigned N, int smooth, int nthreads);
 oracle_mesh *oracle_compute_ses(const float *xyz, const float *rad, unsigned N, float dx,
                                 int smooth, int fp64, int nthreads);
+/* The reference's slicing (-s slice): one mesh per slice box, concatenated as
+ * API_computeSES concatenates them; see qses_oracle.cpp.  NULL for slice < 1. */
+oracle_mesh *oracle_compute_ses_slices(const float *xyz, const float *rad, unsigned N, float dx, int slice,
+                                       int smooth, int fp64, int nthreads);
 void oracle_mesh_free(oracle_mesh *m);
 void oracle_smooth_f32(float *v, unsigned nv, const int32_t *tri, unsigned nt, int passes);
 double oracle_hausdorff(const double *va, unsigned nva, const int32_t *ta, unsigned nta,

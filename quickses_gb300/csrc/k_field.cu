@@ -133,17 +133,23 @@ __device__ __forceinline__ void sas_tile(const QGrid &g, int w, int jb, int ib, 
     __shared__ int s_n, s_over;
     const int j0 = jb * kSasTY, i0 = ib * kSasTX;
     const int t = threadIdx.x, i = i0 + t / kSasTY, j = j0 + t % kSasTY, k0 = w * 32;
-    const int G = g.G, last = G - 2;  // voxels with an index of G-1 are never computed (Kernels.cu:436-441)
+    // Voxels with an index >= lim on an axis are never computed and stay outside: the last
+    // layer G-1 (Kernels.cu:436-441) and, for a slice box, its own last layer and whatever
+    // lies at or past the molecule grid's last layer.  Positions use the grid index
+    // box index + off (gridToSpace of ijkOffset, Kernels.cu:427-446).
+    const int G = g.G, lastx = g.lim[0] - 1, lasty = g.lim[1] - 1, lastz = g.lim[2] - 1;
+    const int oi = g.off[0], oj = g.off[1], ok = g.off[2];
     const unsigned valid = (k0 + 32 <= G) ? 0xffffffffu : ((1u << (G - k0)) - 1u);
-    const unsigned lastbit = (G - 1 >= k0 && G - 1 < k0 + 32) ? (1u << (G - 1 - k0)) : 0u;
-    const int klim = min(k0 + 31, last);
+    const int fz = max(g.lim[2] - k0, 0);  // first forced-outside bit of this word
+    const unsigned forced = fz >= 32 ? 0u : (valid & ~((1u << fz) - 1u));
+    const int klim = min(k0 + 31, lastz);
     const float inv_dx = 1.0f / g.dx;
     unsigned sasw = 0, inw = 0;
 
-    if (i0 <= last && j0 <= last && k0 <= last) {
-        const float bx0 = vox(i0, g.dx, g.ox), bx1 = vox(min(i0 + kSasTX - 1, last), g.dx, g.ox);
-        const float by0 = vox(j0, g.dx, g.oy), by1 = vox(min(j0 + kSasTY - 1, last), g.dx, g.oy);
-        const float bz0 = vox(k0, g.dx, g.oz), bz1 = vox(klim, g.dx, g.oz);
+    if (i0 <= lastx && j0 <= lasty && k0 <= lastz) {
+        const float bx0 = vox(i0 + oi, g.dx, g.ox), bx1 = vox(min(i0 + kSasTX - 1, lastx) + oi, g.dx, g.ox);
+        const float by0 = vox(j0 + oj, g.dx, g.oy), by1 = vox(min(j0 + kSasTY - 1, lasty) + oj, g.dx, g.oy);
+        const float bz0 = vox(k0 + ok, g.dx, g.oz), bz1 = vox(klim + ok, g.dx, g.oz);
         const float ext = g.cell * 1.01f + g.dx;
         auto crange = [&](float lo, float hi, float o, int &c0, int &c1) {
             c0 = min(max((int)floorf((lo - ext - o) / g.cell), 0), g.gnb - 1);
@@ -179,12 +185,14 @@ __device__ __forceinline__ void sas_tile(const QGrid &g, int w, int jb, int ib, 
             }
         }
         __syncthreads();
-        if (i <= last && j <= last) {
-            const float px = vox(i, g.dx, g.ox), py = vox(j, g.dx, g.oy);
+        if (i <= lastx && j <= lasty) {
+            const float px = vox(i + oi, g.dx, g.ox), py = vox(j + oj, g.dx, g.oy);
+            const int kg0 = k0 + ok, kglim = klim + ok;  // z range as grid indices (bits from kg0)
             if (!s_over) {
                 const int na = s_n;
                 for (int q = 0; q < na; q++)
-                    sas_row_atom(px, py, s_x[q], s_y[q], s_z[q], s_tin[q], s_ts[q], k0, klim, g, inv_dx, sasw, inw);
+                    sas_row_atom(px, py, s_x[q], s_y[q], s_z[q], s_tin[q], s_ts[q], kg0, kglim, g, inv_dx, sasw,
+                                 inw);
             } else {
                 // Too many candidates for shared memory: walk the cells directly.
                 for (int c = 0; c < ncell; c++) {
@@ -194,7 +202,7 @@ __device__ __forceinline__ void sas_tile(const QGrid &g, int w, int jb, int ib, 
                         float4 a = atoms[s];
                         float tin, tsas;
                         atom_thresholds(a.w, g, tin, tsas);
-                        sas_row_atom(px, py, a.x, a.y, a.z, tin, tsas, k0, klim, g, inv_dx, sasw, inw);
+                        sas_row_atom(px, py, a.x, a.y, a.z, tin, tsas, kg0, kglim, g, inv_dx, sasw, inw);
                     }
                 }
             }
@@ -202,12 +210,12 @@ __device__ __forceinline__ void sas_tile(const QGrid &g, int w, int jb, int ib, 
     }
     if (i < G && j < G) {
         unsigned outw, inw2;
-        if (i >= G - 1 || j >= G - 1) {
+        if (i > lastx || j > lasty) {
             outw = valid;
             inw2 = 0u;
         } else {
-            outw = (~sasw & valid) | lastbit;
-            inw2 = inw & ~lastbit;
+            outw = (~sasw & valid) | forced;
+            inw2 = inw & ~forced;
         }
         size_t idx = ((size_t)i * G + j) * g.W + w;
         inMask[idx] = inw2;

@@ -57,6 +57,10 @@ __device__ unsigned long long edge_key(const QGrid &g, const unsigned char *__re
 #pragma unroll
     for (int c = 0; c < 3; c++)
         if (c == ax) p[c] = __fmaf_rn(t, __fsub_rn(vox(idx[c] + 1, g.dx, o[c]), p[c]), p[c]);
+    if (g.off[0] | g.off[1] | g.off[2]) {  // a slice box: + offset * dx (MarchingCubes.cu:841-848)
+#pragma unroll
+        for (int c = 0; c < 3; c++) p[c] = __fadd_rn(p[c], __fmul_rn((float)g.off[c], g.dx));
+    }
     // groupVertices: round(v / 0.001) (MarchingCubes.cu:859)
     long long mx = (long long)roundf(__fdiv_rn(p[0], QSES_WELD_TOL));
     long long my = (long long)roundf(__fdiv_rn(p[1], QSES_WELD_TOL));
@@ -97,6 +101,15 @@ __device__ __forceinline__ unsigned grp_incl_scan(unsigned v, int sub, int Lg) {
 // calls this (groups whose row is past the end pass valid = false and write nothing).
 // Edge keys get `keyhi` added (the molecule's slot above the local key bits in a batch, 0
 // for a single molecule).
+// Bits [a, b) of a 32-bit word, the bounds clamped to [0, 32].
+__device__ __forceinline__ unsigned bits_in(int a, int b) {
+    a = max(a, 0);
+    b = min(b, 32);
+    if (a >= b) return 0u;
+    const unsigned below_b = b == 32 ? 0xffffffffu : ((1u << b) - 1u);
+    return below_b & ~((1u << a) - 1u);
+}
+
 // Words per lane record of the triangle pass (34 used; an odd stride spreads the lanes'
 // writes over the shared-memory banks).
 constexpr int kRecW = 35;
@@ -117,7 +130,14 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
     const int Gc = g.Gc, E = Gc + 1;
     if (!valid) row = 0;
     const int i = (int)(row / E), j = (int)(row % E);
-    const bool cellsRow = valid && i < Gc && j < Gc;
+    // Emitted cells: [clo, chi) per axis (the whole grid: [0, Gc)).  A row's +x edges are
+    // used when a cell of the range has them (x in [clo, chi), y in [clo, chi]), likewise +y;
+    // its +z edges when x and y are in [clo, chi].
+    const int lox = g.clo[0], hix = g.chi[0], loy = g.clo[1], hiy = g.chi[1], loz = g.clo[2], hiz = g.chi[2];
+    auto xr = [&](int a, int b) { return a >= lox && a < hix && b >= loy && b <= hiy; };
+    auto yr = [&](int a, int b) { return a >= lox && a <= hix && b >= loy && b < hiy; };
+    auto zr = [&](int a, int b) { return a >= lox && a <= hix && b >= loy && b <= hiy; };
+    const bool cellsRow = valid && i >= lox && i < hix && j >= loy && j < hiy;
     const int Wc = (Gc + 32) / 32;  // words holding voxels 0..Gc
 
     unsigned triBase = 0, eb0 = 0, eb1 = 0, eb2 = 0, eb3 = 0;  // owners (0,0) (0,1) (1,0) (1,1)
@@ -135,20 +155,18 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
         const int kb = w * 32;
         unsigned kv = 0u, kc = 0u;
         if (act) {
-            int nvx = Gc - kb + 1;  // voxels kb..Gc
-            kv = nvx >= 32 ? 0xffffffffu : ((1u << nvx) - 1u);
-            int ncl = Gc - kb;      // cells / z-edges kb..Gc-1
-            kc = ncl >= 32 ? 0xffffffffu : (ncl <= 0 ? 0u : ((1u << ncl) - 1u));
+            kv = bits_in(loz - kb, hiz - kb + 1);  // voxels in [loz, hiz]
+            kc = bits_in(loz - kb, hiz - kb);      // cells / z-edges in [loz, hiz)
         }
-        const bool nxt = act && (kb + 32 <= Gc);
+        const bool nxt = act && (kb + 32 <= hiz) && (kb + 32 >= loz);
         auto L = [&](int a, int b, int ww) { return act ? ld_sign(sign, g, i + a, j + b, ww) : 0u; };
         const unsigned S00 = L(0, 0, w), S10 = L(1, 0, w), S01 = L(0, 1, w), S11 = L(1, 1, w);
         const unsigned N00 = L(0, 0, w + 1), N10 = L(1, 0, w + 1), N01 = L(0, 1, w + 1), N11 = L(1, 1, w + 1);
         const unsigned P00 = (S00 >> 1) | (N00 << 31), P10 = (S10 >> 1) | (N10 << 31);
         const unsigned P01 = (S01 >> 1) | (N01 << 31), P11 = (S11 >> 1) | (N11 << 31);
-        const unsigned X00 = i < Gc ? (S00 ^ S10) & kv : 0u;
-        const unsigned Y00 = j < Gc ? (S00 ^ S01) & kv : 0u;
-        const unsigned Z00 = (S00 ^ P00) & kc;
+        const unsigned X00 = xr(i, j) ? (S00 ^ S10) & kv : 0u;
+        const unsigned Y00 = yr(i, j) ? (S00 ^ S01) & kv : 0u;
+        const unsigned Z00 = zr(i, j) ? (S00 ^ P00) & kc : 0u;
         const unsigned c00 = __popc(X00) + __popc(Y00) + __popc(Z00);
         unsigned cellm = 0u, ntri = 0u, nt0 = 0u, nt1 = 0u, nt2 = 0u;  // nt bit k of each active cell
         if (cellsRow) {
@@ -173,24 +191,23 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
         // Edges owned by the three neighbouring rows, for triangle corners.
         const unsigned S20 = L(2, 0, w), S21 = L(2, 1, w), S02 = L(0, 2, w), S12 = L(1, 2, w);
         const unsigned N20 = L(2, 0, w + 1), N21 = L(2, 1, w + 1), N02 = L(0, 2, w + 1), N12 = L(1, 2, w + 1);
-        const bool r1 = j + 1 <= Gc, r2 = i + 1 <= Gc, r3 = r1 && r2;
-        const unsigned X01 = (r1 && i < Gc) ? (S01 ^ S11) & kv : 0u;
-        const unsigned Y01 = (j + 1 < Gc) ? (S01 ^ S02) & kv : 0u;
-        const unsigned Z01 = r1 ? (S01 ^ P01) & kc : 0u;
-        const unsigned X10 = (i + 1 < Gc) ? (S10 ^ S20) & kv : 0u;
-        const unsigned Y10 = (r2 && j < Gc) ? (S10 ^ S11) & kv : 0u;
-        const unsigned Z10 = r2 ? (S10 ^ P10) & kc : 0u;
-        const unsigned X11 = (r1 && i + 1 < Gc) ? (S11 ^ S21) & kv : 0u;
-        const unsigned Y11 = (r2 && j + 1 < Gc) ? (S11 ^ S12) & kv : 0u;
-        const unsigned Z11 = r3 ? (S11 ^ P11) & kc : 0u;
+        const unsigned X01 = xr(i, j + 1) ? (S01 ^ S11) & kv : 0u;
+        const unsigned Y01 = yr(i, j + 1) ? (S01 ^ S02) & kv : 0u;
+        const unsigned Z01 = zr(i, j + 1) ? (S01 ^ P01) & kc : 0u;
+        const unsigned X10 = xr(i + 1, j) ? (S10 ^ S20) & kv : 0u;
+        const unsigned Y10 = yr(i + 1, j) ? (S10 ^ S11) & kv : 0u;
+        const unsigned Z10 = zr(i + 1, j) ? (S10 ^ P10) & kc : 0u;
+        const unsigned X11 = xr(i + 1, j + 1) ? (S11 ^ S21) & kv : 0u;
+        const unsigned Y11 = yr(i + 1, j + 1) ? (S11 ^ S12) & kv : 0u;
+        const unsigned Z11 = zr(i + 1, j + 1) ? (S11 ^ P11) & kc : 0u;
         const unsigned c01 = __popc(X01) + __popc(Y01) + __popc(Z01);
         const unsigned c10 = __popc(X10) + __popc(Y10) + __popc(Z10);
         const unsigned c11 = __popc(X11) + __popc(Y11) + __popc(Z11);
         // Activity of the x/y edges of voxel kb+32 (bit 0 of the next word).
-        const unsigned xn0 = (nxt && i < Gc) ? ((N00 ^ N10) & 1u) : 0u, yn0 = (nxt && j < Gc) ? ((N00 ^ N01) & 1u) : 0u;
-        const unsigned xn1 = (nxt && r1 && i < Gc) ? ((N01 ^ N11) & 1u) : 0u, yn1 = (nxt && j + 1 < Gc) ? ((N01 ^ N02) & 1u) : 0u;
-        const unsigned xn2 = (nxt && i + 1 < Gc) ? ((N10 ^ N20) & 1u) : 0u, yn2 = (nxt && r2 && j < Gc) ? ((N10 ^ N11) & 1u) : 0u;
-        const unsigned xn3 = (nxt && r1 && i + 1 < Gc) ? ((N11 ^ N21) & 1u) : 0u, yn3 = (nxt && r2 && j + 1 < Gc) ? ((N11 ^ N12) & 1u) : 0u;
+        const unsigned xn0 = (nxt && xr(i, j)) ? ((N00 ^ N10) & 1u) : 0u, yn0 = (nxt && yr(i, j)) ? ((N00 ^ N01) & 1u) : 0u;
+        const unsigned xn1 = (nxt && xr(i, j + 1)) ? ((N01 ^ N11) & 1u) : 0u, yn1 = (nxt && yr(i, j + 1)) ? ((N01 ^ N02) & 1u) : 0u;
+        const unsigned xn2 = (nxt && xr(i + 1, j)) ? ((N10 ^ N20) & 1u) : 0u, yn2 = (nxt && yr(i + 1, j)) ? ((N10 ^ N11) & 1u) : 0u;
+        const unsigned xn3 = (nxt && xr(i + 1, j + 1)) ? ((N11 ^ N21) & 1u) : 0u, yn3 = (nxt && yr(i + 1, j + 1)) ? ((N11 ^ N12) & 1u) : 0u;
 
         const unsigned p0 = grp_incl_scan(c00, sub, Lg) - c00, p1 = grp_incl_scan(c01, sub, Lg) - c01;
         const unsigned p2 = grp_incl_scan(c10, sub, Lg) - c10, p3 = grp_incl_scan(c11, sub, Lg) - c11;

@@ -71,6 +71,12 @@ int grid_from_bounds(const float mn_in[3], const float mx_in[3], float maxR_in, 
     if (g.G - g.R - 1 >= 0) lim = std::min(lim, g.G - g.R - 1);
     if (g.G - 2 * g.R - 1 >= 0) lim = std::min(lim, g.G - 2 * g.R - 1);
     g.Gc = std::max(lim, 0);
+    for (int a = 0; a < 3; a++) {
+        g.off[a] = 0;
+        g.lim[a] = g.G - 1;  // Kernels.cu:436-441: the last layer is never computed
+        g.clo[a] = 0;
+        g.chi[a] = g.Gc;
+    }
     g.W = (g.G + 31) / 32;
     g.Gp = 32 * g.W;
     // Code values and the first negative one (the value is non-increasing in n).

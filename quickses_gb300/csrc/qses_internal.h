@@ -33,6 +33,13 @@ struct QGrid {
     unsigned N;        // atoms
     long long bx, by, bz;  // weld key base (quantised origin - margin)
     long long Rq;          // weld key radix per axis
+    // A box of the reference's slicing (else the whole grid: offsets 0, limits G - 1, cell
+    // ranges [0, Gc)).  Voxel (i, j, k) of the box is voxel (i + off[0], j + off[1],
+    // k + off[2]) of the molecule's grid: SAS positions use the grid index, vertex positions
+    // the box index plus off * dx (CudaSurf.cu:671-682, MarchingCubes.cu:841-848).
+    int off[3];
+    int lim[3];        // voxels with a box index >= lim[a] on any axis a stay outside
+    int clo[3], chi[3];  // marching-cubes cells emitted per axis: [clo, chi), chi <= Gc
 };
 
 // One molecule of a batch: its grid and where its pieces sit in the batch's concatenated
