@@ -91,12 +91,25 @@ typedef struct qses_context qses_context;
 typedef struct {
     float voxel;        /* SES voxel size in A (CLI -v, default 0.5) */
     int smooth_passes;  /* Laplacian passes (CLI -l, default 1) */
-    int slice;          /* CLI -s: x-slab thickness in voxels for the field (memory
-                           schedule only; the mesh does not depend on it), default 300 */
+    int slice;          /* CLI -s: slice size in voxels, default 300; used only with
+                           QSES_FLAG_REFERENCE_SLICES (the reference's slicing) */
     int flags;          /* QSES_FLAG_* */
 } qses_params;
 
 #define QSES_FLAG_KEEP_DEGENERATE 1  /* keep triangles with a repeated index (CLI/OBJ path) */
+/* The reference's slicing, for diffs against meshes QuickSES wrote (CudaSurf.cu:629-754,
+ * the executable's -s): the grid is cut into cores of `slice` voxels, each computed in a
+ * box reaching R voxels before it (refine windows clamped to the box, the box's last layer
+ * outside), each slice's cells emitted by the reference's rules (two cell layers at every
+ * seam from both sides), meshed, welded, given closest atoms and smoothed on its own; the
+ * meshes are concatenated with vertex ids offset slice by slice, as API_computeSES does.
+ * The reference never writes a slice's last triangle (MarchingCubes.cu:845 with
+ * CudaSurf.cu:421) and leaves whatever the device memory held in its three vertices; here
+ * that triangle and any vertex only it used are left out.  qses_compute only (host mesh);
+ * device memory is bounded by one slice box, so grids of any size within 1290 neighbour
+ * cells per axis are accepted.  Without this flag the result is the reference's output
+ * for one slice covering the grid (slice >= grid size), whatever `slice` is. */
+#define QSES_FLAG_REFERENCE_SLICES 2
 
 typedef struct {
     unsigned n_vertices;
@@ -122,6 +135,10 @@ QSES_API void qses_params_default(qses_params *p);
 QSES_API int qses_compute(qses_context *ctx, const qses_params *p, const qses_float3 *atoms,
                           const float *radii, unsigned n, qses_mesh *out);
 QSES_API void qses_mesh_release(qses_mesh *m);
+/* Per-slice vertex and triangle counts of the last qses_compute in the reference's slicing
+ * mode (slices with a mesh, in the reference's order: x outermost); returns the number of
+ * slices (at most `max` written), 0 after any other call. */
+QSES_API int qses_last_slices(qses_context *ctx, unsigned *n_vertices, unsigned *n_triangles, int max);
 
 /* Device-resident form: atoms already in device memory (3n floats, n floats); the mesh
  * stays on the device in the context's workspace (valid until the next call on `ctx`).

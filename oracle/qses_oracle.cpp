@@ -498,6 +498,23 @@ size_t box_codes(const oracle_grid *g, const Atoms &A, int D, const int off[3], 
                 cls[i * D2 + (size_t)j * D + k] =
                     kept ? 0 : (uint8_t)sas_class<P>(off[0] + i, off[1] + j, off[2] + k, g, A, tin, tsas);
             }
+    /* Summed-area table of "outside" for O(1) empty-window tests. */
+    const size_t P1 = (size_t)D + 1;
+    std::vector<int32_t> sat(P1 * P1 * P1, 0);
+    for (int i = 0; i < D; i++)
+        for (int j = 0; j < D; j++)
+            for (int k = 0; k < D; k++) {
+                const int o = cls[i * D2 + (size_t)j * D + k] == 0;
+                const size_t a = ((size_t)(i + 1) * P1 + (j + 1)) * P1 + (k + 1);
+                sat[a] = o + sat[a - 1] + sat[a - P1] + sat[a - P1 * P1] - sat[a - P1 - 1] - sat[a - P1 * P1 - 1] -
+                         sat[a - P1 * P1 - P1] + sat[a - P1 * P1 - P1 - 1];
+            }
+    auto outside_in = [&](int i0, int i1, int j0, int j1, int k0, int k1) {  // inclusive bounds
+        auto S_ = [&](int a, int b, int c) { return sat[((size_t)a * P1 + b) * P1 + c]; };
+        i1++; j1++; k1++;
+        return S_(i1, j1, k1) - S_(i0, j1, k1) - S_(i1, j0, k1) - S_(i1, j1, k0) + S_(i0, j0, k1) + S_(i0, j1, k0) +
+               S_(i1, j0, k0) - S_(i0, j0, k0);
+    };
     struct Off { int di, dj, dk, n; };
     std::vector<Off> offs;
     for (int a = -R; a <= R; a++)
@@ -514,6 +531,11 @@ size_t box_codes(const oracle_grid *g, const Atoms &A, int D, const int off[3], 
                 if (c == 1) {
                     border++;
                     code = ORACLE_CODE_NONE;
+                    if (outside_in(std::max(i - R, 0), std::min(i + R, D - 1), std::max(j - R, 0),
+                                   std::min(j + R, D - 1), std::max(k - R, 0), std::min(k + R, D - 1)) == 0) {
+                        codes[i * D2 + (size_t)j * D + k] = code;
+                        continue;
+                    }
                     for (const Off &o : offs) {
                         const int a = i + o.di, b = j + o.dj, d = k + o.dk;
                         if (a < 0 || b < 0 || d < 0 || a >= D || b >= D || d >= D) continue;

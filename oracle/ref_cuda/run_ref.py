@@ -8,6 +8,7 @@ TEST INFRASTRUCTURE ONLY.  Needs oracle/_ref/libQuickSES.so and oracle/_ref/libr
     python oracle/ref_cuda/run_ref.py fixtures                 # tests/golden/ref_cuda.npz
     python oracle/ref_cuda/run_ref.py stream batched|trajectory|served   # plain path, molecules/s
     python oracle/ref_cuda/run_ref.py smooth ball50k           # SmoothMesh.cpp on the CPU vs ours
+    python oracle/ref_cuda/run_ref.py slices                   # tests/golden/ref_slices.npz
     python oracle/ref_cuda/run_ref.py bench ball50k 3          # the reference alone: wall clock of
                                                                # API_computeSES (bench.py's ref_cuda)
 
@@ -287,6 +288,50 @@ def stream(which, limit=None):
                       "ref_molecules_per_s": len(reqs) / total, "ref_voxels_per_s": vox / total}), flush=True)
 
 
+# Molecules of the per-slice fixtures: (atoms, seed, voxel, slice, smoothing passes).  Small
+# slices give many slices on small molecules; voxel 0.75 A has R = 2, where the reference
+# emits no cell of any slice that does not start at 0 (MarchingCubes.cu:585-590).
+SLICE_CASES = [(150, 91, 0.5, 16, (0, 1)), (120, 92, 0.4, 20, (0, 1)), (100, 93, 0.3, 24, (0,)),
+               (150, 94, 0.75, 16, (0,))]
+
+
+def slices(out=os.path.join(ROOT, "tests", "golden", "ref_slices.npz")):
+    """The reference's own per-slice meshes (computeSlicedSES with its SLICE set), through
+    oracle/_ref/libref_slices.so: per case and pass count, every slice's vertices, triangles
+    (its unwritten last triangle included) and sorted atom ids, concatenated, with counts."""
+    L = ctypes.CDLL(os.path.join(REF, "libref_slices.so"))
+    L.ref_slices_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_float, ctypes.c_int,
+                                 ctypes.c_int]
+    L.ref_slices_counts.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.ref_slices_copy.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    data = {}
+    for ci, (n, seed, dx, sl, passes) in enumerate(SLICE_CASES):
+        xyz, rad = O.synth_ball(n, seed)
+        p = "s%d_" % ci
+        data[p + "xyz"], data[p + "rad"] = xyz, rad
+        data[p + "dx"], data[p + "slice"] = np.float32(dx), np.int32(sl)
+        for sm in passes:
+            ns = L.ref_slices_run(xyz.ctypes.data, rad.ctypes.data, n, ctypes.c_float(dx), sl, sm)
+            vs, ts, as_, cnt = [], [], [], []
+            for k in range(ns):
+                nv, nt = ctypes.c_int(), ctypes.c_int()
+                L.ref_slices_counts(k, ctypes.byref(nv), ctypes.byref(nt))
+                v = np.zeros((nv.value, 3), np.float32)
+                t = np.zeros((nt.value, 3), np.int32)
+                a = np.zeros(nv.value, np.int32)
+                L.ref_slices_copy(k, v.ctypes.data, t.ctypes.data, a.ctypes.data)
+                vs.append(v); ts.append(t); as_.append(a); cnt.append((nv.value, nt.value))
+            q = p + "p%d_" % sm
+            data[q + "counts"] = np.array(cnt, np.int32).reshape(-1, 2)
+            data[q + "v"] = np.concatenate(vs) if vs else np.zeros((0, 3), np.float32)
+            data[q + "t"] = np.concatenate(ts) if ts else np.zeros((0, 3), np.int32)
+            data[q + "a"] = np.concatenate(as_) if as_ else np.zeros(0, np.int32)
+            print(json.dumps({"case": ci, "passes": sm, "slices": ns, "vertices": int(sum(c[0] for c in cnt)),
+                              "triangles": int(sum(c[1] for c in cnt))}), flush=True)
+    np.savez_compressed(out, **data)
+    print("wrote", out, os.path.getsize(out))
+
+
 def bench(name, calls):
     """The reference's API_computeSES alone on one workload: one untimed call, then `calls`
     timed ones (wall clock around the library call, host atoms in, mesh in its host
@@ -327,3 +372,5 @@ if __name__ == "__main__":
         field()
     elif mode == "fixtures":
         fixtures()
+    elif mode == "slices":
+        slices(*sys.argv[2:3])

@@ -22,7 +22,7 @@ NVCC = ["nvcc", "-std=c++17", "-O3", "-lineinfo"] + ARCH + [
 GXX = ["g++", "-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off",
        "-I", "/usr/local/cuda/include", "-I", CSRC, "-I", INCLUDE]
 
-LIB_CU = ["k_prims.cu", "k_field.cu", "k_hash.cu", "k_mesh.cu", "k_smooth.cu", "pipeline.cu", "pipeline_batch.cu", "noalloc.cu"]
+LIB_CU = ["k_prims.cu", "k_field.cu", "k_hash.cu", "k_mesh.cu", "k_smooth.cu", "pipeline.cu", "pipeline_batch.cu", "pipeline_slices.cu", "noalloc.cu"]
 # Per-file flags: the atom cell key uses the reference's own arithmetic (see k_hash.cu).
 EXTRA_FLAGS = {"k_hash.cu": ["-use_fast_math"]}
 LIB_CPP = ["api.cpp", "synth.cpp", "io.cpp", "server.cpp"]

@@ -18,6 +18,7 @@ QSES_ERR_TIMEOUT = 6
 QSES_ERR_INTERNAL = 7
 QSES_ERR_CANCELLED = 8
 QSES_FLAG_KEEP_DEGENERATE = 1
+QSES_FLAG_REFERENCE_SLICES = 2
 
 
 class Float3(ctypes.Structure):
@@ -78,6 +79,7 @@ SIGNATURES = {
     "qses_context_destroy": (ctypes.c_int, [_VP]),
     "qses_params_default": (None, [ctypes.POINTER(Params)]),
     "qses_compute": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _FP, ctypes.c_uint, ctypes.POINTER(Mesh)]),
+    "qses_last_slices": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
     "qses_mesh_release": (None, [ctypes.POINTER(Mesh)]),
     "qses_compute_device": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _VP, ctypes.c_uint,
                                            ctypes.POINTER(DeviceMesh)]),

@@ -57,7 +57,8 @@ def _requests(requests):
         reqs[i].atoms, reqs[i].radii, reqs[i].n = xyz.ctypes.data, rad.ctypes.data, xyz.shape[0]
         reqs[i].voxel = float(r.get("voxel", 0.5))
         reqs[i].smooth_passes = int(r.get("smooth", 1))
-        reqs[i].flags = L.QSES_FLAG_KEEP_DEGENERATE if r.get("keep_degenerate", False) else 0
+        reqs[i].flags = (L.QSES_FLAG_KEEP_DEGENERATE if r.get("keep_degenerate", False) else 0) | \
+            int(r.get("flags", 0))
     return arrays, reqs
 
 
@@ -100,27 +101,32 @@ class Context:
     def handle(self):
         return self._h
 
-    def _params(self, voxel, smooth, keep_degenerate, slice_):
+    def _params(self, voxel, smooth, keep_degenerate, slice_, reference_slices=False):
         p = L.Params()
         self._lib.qses_params_default(ctypes.byref(p))
         p.voxel = float(voxel)
         p.smooth_passes = int(smooth)
         p.slice = int(slice_)
-        p.flags = L.QSES_FLAG_KEEP_DEGENERATE if keep_degenerate else 0
+        p.flags = (L.QSES_FLAG_KEEP_DEGENERATE if keep_degenerate else 0) | \
+            (L.QSES_FLAG_REFERENCE_SLICES if reference_slices else 0)
         return p
 
     def _check(self, rc, what):
         if rc != L.QSES_OK:
             raise QSESError(rc, "%s: %s" % (what, self._lib.qses_last_error(self._h).decode()))
 
-    def compute(self, xyz, radii, voxel=0.5, smooth=1, keep_degenerate=False, slice=300) -> Mesh:
-        """Atoms (N, 3) + radii (N,) on the host -> welded, smoothed mesh on the host."""
+    def compute(self, xyz, radii, voxel=0.5, smooth=1, keep_degenerate=False, slice=300,
+                reference_slices=False) -> Mesh:
+        """Atoms (N, 3) + radii (N,) on the host -> welded, smoothed mesh on the host.
+        reference_slices: the reference's per-slice output for slices of `slice` voxels
+        (QSES_FLAG_REFERENCE_SLICES); slice_counts() then gives each slice's counts."""
         xyz = _f32(xyz, 3)
         radii = _f32(radii)
         if radii.shape != (xyz.shape[0],):
             raise ValueError("radii must have shape (N,)")
         m = L.Mesh()
-        rc = self._lib.qses_compute(self._h, ctypes.byref(self._params(voxel, smooth, keep_degenerate, slice)),
+        rc = self._lib.qses_compute(self._h, ctypes.byref(self._params(voxel, smooth, keep_degenerate, slice,
+                                                                       reference_slices)),
                                     xyz.ctypes.data_as(ctypes.c_void_p),
                                     radii.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), xyz.shape[0],
                                     ctypes.byref(m))
@@ -130,6 +136,14 @@ class Context:
         finally:
             self._lib.qses_mesh_release(ctypes.byref(m))
         return out
+
+    def slice_counts(self):
+        """(vertices, triangles) per slice of the last call in the reference's slicing mode."""
+        k = self._lib.qses_last_slices(self._h, None, None, 0)
+        nv = (ctypes.c_uint * max(1, k))()
+        nt = (ctypes.c_uint * max(1, k))()
+        self._lib.qses_last_slices(self._h, nv, nt, k)
+        return [(int(nv[i]), int(nt[i])) for i in range(k)]
 
     def compute_batch(self, requests):
         """Batch form: `requests` is a list of dicts with keys xyz, radii and optionally

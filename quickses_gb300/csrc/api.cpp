@@ -182,6 +182,40 @@ int check_params(qses_context *ctx, const qses_params *p) {
     if (!(p->voxel > 0.0f)) return ctx->fail(QSES_ERR_INVALID_ARG, "voxel size must be > 0");
     if (p->smooth_passes < 0 || p->smooth_passes > 1000)
         return ctx->fail(QSES_ERR_INVALID_ARG, "smooth_passes must be in [0, 1000]");
+    if ((p->flags & QSES_FLAG_REFERENCE_SLICES) && p->slice < 1)
+        return ctx->fail(QSES_ERR_INVALID_ARG, "slice must be >= 1");
+    return QSES_OK;
+}
+
+// The concatenated meshes of the reference's slicing mode into one pinned block.
+int host_mesh_from_slices(qses_context *ctx, const qses::SlicedMesh &sm, qses_mesh *out) {
+    memset(out, 0, sizeof(*out));
+    const unsigned nv = (unsigned)(sm.vertices.size() / 3), nt = (unsigned)(sm.triangles.size() / 3);
+    const size_t vb = 12ull * nv, tb = 12ull * nt, ab = 4ull * nv;
+    HostMesh *hm = new (std::nothrow) HostMesh();
+    if (!hm) return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "host mesh");
+    hm->block = pinned_pool().take(vb + tb + 2 * ab + 64, &hm->bytes);
+    if (!hm->block) {
+        delete hm;
+        return ctx->fail(QSES_ERR_OUT_OF_MEMORY, "pinned host mesh");
+    }
+    char *b = (char *)hm->block;
+    if (vb) memcpy(b, sm.vertices.data(), vb);
+    if (tb) memcpy(b + vb, sm.triangles.data(), tb);
+    if (ab) {
+        memcpy(b + vb + tb, sm.atom_sorted.data(), ab);
+        memcpy(b + vb + tb + ab, sm.atom_input.data(), ab);
+    }
+    out->vertices = (qses_float3 *)b;
+    out->triangles = (int *)(b + vb);
+    out->atom_sorted = (int *)(b + vb + tb);
+    out->atom_input = (int *)(b + vb + tb + ab);
+    out->n_vertices = nv;
+    out->n_triangles = nt;
+    out->grid_dim = ctx->grid.G;
+    out->origin[0] = ctx->grid.ox; out->origin[1] = ctx->grid.oy; out->origin[2] = ctx->grid.oz;
+    out->_owner = hm;
+    ctx->last_d2h = vb + tb + 2 * ab;
     return QSES_OK;
 }
 
@@ -297,6 +331,12 @@ QSES_API int qses_compute(qses_context *ctx, const qses_params *p, const qses_fl
     cudaError_t e = cudaMemcpyAsync(d_xyz, atoms, 12ull * n, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_r, radii, 4ull * n, cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) return ctx->fail(QSES_ERR_CUDA, "atom upload", e);
+    if (p->flags & QSES_FLAG_REFERENCE_SLICES) {
+        qses::SlicedMesh sm;
+        rc = qses::run_pipeline_slices(ctx, *p, d_xyz, d_r, n, sm);
+        if (rc) return rc;
+        return host_mesh_from_slices(ctx, sm, out);
+    }
     ctx->dl = qses::HostDownload();
     ctx->dl.want = true;
     rc = qses::run_pipeline(ctx, *p, d_xyz, d_r, n);
@@ -340,6 +380,8 @@ QSES_API int qses_compute_device(qses_context *ctx, const qses_params *p, const 
     memset(out, 0, sizeof(*out));
     int rc = check_params(ctx, p);
     if (rc) return rc;
+    if (p->flags & QSES_FLAG_REFERENCE_SLICES)
+        return ctx->fail(QSES_ERR_UNSUPPORTED, "the reference's slicing mode returns host meshes (qses_compute)");
     cudaSetDevice(ctx->device);
     if (n <= 1) {
         ctx->mesh = DeviceMesh();
@@ -356,6 +398,16 @@ QSES_API int qses_compute_device(qses_context *ctx, const qses_params *p, const 
     out->d_atom_sorted = ctx->mesh.atom_sorted;
     out->d_atom_input = ctx->mesh.atom_input;
     return QSES_OK;
+}
+
+QSES_API int qses_last_slices(qses_context *ctx, unsigned *n_vertices, unsigned *n_triangles, int max) {
+    if (!ctx) return -1;
+    const int k = (int)ctx->slice_nv.size();
+    for (int q = 0; q < k && q < max; q++) {
+        if (n_vertices) n_vertices[q] = ctx->slice_nv[q];
+        if (n_triangles) n_triangles[q] = ctx->slice_nt[q];
+    }
+    return k;
 }
 
 QSES_API void qses_mesh_release(qses_mesh *m) {
@@ -462,6 +514,8 @@ QSES_API int qses_compute_batch(qses_context *ctx, const qses_request *reqs, uns
         int rc = QSES_OK;
         if (!(r.voxel > 0.0f) || r.smooth_passes < 0 || r.smooth_passes > 1000 || (r.n > 0 && (!r.atoms || !r.radii)))
             rc = QSES_ERR_INVALID_ARG;
+        else if (r.flags & QSES_FLAG_REFERENCE_SLICES)
+            rc = QSES_ERR_UNSUPPORTED;  // a per-molecule compatibility mode (qses_compute)
         else if (r.n > 1)
             rc = size_request(r, grids[i]);
         if (status) status[i] = rc;

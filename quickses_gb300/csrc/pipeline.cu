@@ -31,7 +31,7 @@ static float code_value(float probe, float dx, int n) {
 }
 
 int grid_from_bounds(const float mn_in[3], const float mx_in[3], float maxR_in, unsigned n, float dx, QGrid &g,
-                     qses_grid_info *info, std::string *why) {
+                     qses_grid_info *info, std::string *why, bool sliced) {
     if (!(dx > 0.0f) || !std::isfinite(dx)) {
         if (why) *why = "voxel size must be a positive finite number";
         return QSES_ERR_INVALID_ARG;
@@ -55,8 +55,12 @@ int grid_from_bounds(const float mn_in[3], const float mx_in[3], float maxR_in, 
     g.probe = probe;
     g.N = n;
     const double gnb_f = std::ceil(maxDist / g.cell), G_f = std::ceil(maxDist / dx), R_f = std::ceil(probe / dx);
-    if (!(gnb_f >= 1 && gnb_f <= 1290 && G_f >= 1 && G_f <= 4096)) {
-        if (why) *why = "grid too large (more than 4096 voxels or 1290 neighbour cells per axis)";
+    // A sliced grid is only ever held one slice box at a time, so only its neighbour cells
+    // bound it.
+    const double G_max = sliced ? 1048576.0 : 4096.0;
+    if (!(gnb_f >= 1 && gnb_f <= 1290 && G_f >= 1 && G_f <= G_max)) {
+        if (why) *why = sliced ? "grid too large (more than 1290 neighbour cells per axis)"
+                               : "grid too large (more than 4096 voxels or 1290 neighbour cells per axis)";
         return QSES_ERR_UNSUPPORTED;
     }
     g.gnb = (int)gnb_f;
@@ -96,7 +100,7 @@ int grid_from_bounds(const float mn_in[3], const float mx_in[3], float maxR_in, 
         return QSES_ERR_UNSUPPORTED;
     }
     g.Rq = (long long)std::ceil(extent / 0.001) + 64;
-    if (g.Rq >= (1ll << 21)) {
+    if (!sliced && g.Rq >= (1ll << 21)) {  // a slice box gets its own key base and radix
         if (why) *why = "grid extent above 2000 A is not supported by the 63-bit weld key";
         return QSES_ERR_UNSUPPORTED;
     }
@@ -615,21 +619,9 @@ static int enqueue_finish(qses_context *ctx, const FinishSeg &c, SegOut &o) {
     return QSES_OK;
 }
 
-int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n) {
+int molecule_grid(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n, QGrid &g,
+                  bool sliced) {
     cudaStream_t s = ctx->stream;
-    QSES_SEG_TRACE("molecule: %u atoms, voxel %.3f, %d passes\n", n, p.voxel, p.smooth_passes);
-    memset(ctx->timeline, 0, sizeof(ctx->timeline));
-    ctx->tick(-1);
-    ctx->launches = 0;
-    for (auto &m : ctx->marks) cudaEventDestroy(m.second);
-    ctx->marks.clear();
-    ctx->mesh = DeviceMesh();
-    ctx->have_grid = false;
-    memset(ctx->diag, 0, sizeof(ctx->diag));
-    QCHK(cudaMemsetAsync((char *)ctx->small + 256, 0, 64, ctx->stream));
-    ctx->mark("start");
-
-    // ---- bounds (one read-back) and sizing on the host
     unsigned *d_mm = (unsigned *)ctx->small;
     int *d_err = (int *)((char *)ctx->small + 64);
     QCHK(cudaMemsetAsync(d_mm, 0xff, 3 * sizeof(unsigned), s));  // min encodings start high
@@ -649,12 +641,35 @@ int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, co
     };
     float mn[3] = {dec(h_mm[0]), dec(h_mm[1]), dec(h_mm[2])}, mx[3] = {dec(h_mm[3]), dec(h_mm[4]), dec(h_mm[5])};
     float maxR = dec(h_mm[6]);
-    QGrid g;
     std::string why;
-    int rc = grid_from_bounds(mn, mx, maxR, n, p.voxel, g, &ctx->info, &why);
+    int rc = grid_from_bounds(mn, mx, maxR, n, p.voxel, g, &ctx->info, &why, sliced);
     if (rc != QSES_OK) return ctx->fail(rc, why.c_str());
     ctx->grid = g;
     ctx->have_grid = true;
+    return QSES_OK;
+}
+
+int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n) {
+    cudaStream_t s = ctx->stream;
+    QSES_SEG_TRACE("molecule: %u atoms, voxel %.3f, %d passes\n", n, p.voxel, p.smooth_passes);
+    memset(ctx->timeline, 0, sizeof(ctx->timeline));
+    ctx->tick(-1);
+    ctx->launches = 0;
+    for (auto &m : ctx->marks) cudaEventDestroy(m.second);
+    ctx->marks.clear();
+    ctx->mesh = DeviceMesh();
+    ctx->have_grid = false;
+    ctx->slice_nv.clear();
+    ctx->slice_nt.clear();
+    memset(ctx->diag, 0, sizeof(ctx->diag));
+    QCHK(cudaMemsetAsync((char *)ctx->small + 256, 0, 64, ctx->stream));
+    ctx->mark("start");
+
+    // ---- bounds (one read-back) and sizing on the host
+    QGrid g;
+    QCHK_RC(molecule_grid(ctx, p, d_xyz, d_r, n, g, false));
+    int *d_err = (int *)((char *)ctx->small + 64);
+    int rc = QSES_OK;
 
     // ---- field workspace
     const size_t ncell = (size_t)g.gnb * g.gnb * g.gnb;

@@ -288,6 +288,8 @@ int run_batch(qses_context *ctx, const BatchItem *items, unsigned count, int pas
     ctx->marks.clear();
     ctx->mesh = DeviceMesh();
     ctx->have_grid = false;
+    ctx->slice_nv.clear();
+    ctx->slice_nt.clear();
     BatchResult &R = ctx->batch;
     R = BatchResult();
     if (count == 0) return QSES_OK;

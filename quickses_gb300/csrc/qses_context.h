@@ -37,8 +37,10 @@ struct DeviceMesh {
     unsigned *sorted_to_input = nullptr, *sorted_keys = nullptr;
 };
 
+// sliced: the grid of the reference's slicing mode, held one slice box at a time (no
+// whole-grid size or weld-key extent limit).
 int grid_from_bounds(const float mn[3], const float mx[3], float maxR, unsigned n, float dx, QGrid &g,
-                     qses_grid_info *info, std::string *why);
+                     qses_grid_info *info, std::string *why, bool sliced = false);
 void fill_lut(const QGrid &g, float *lut);
 
 // One molecule of a batch call: host atoms and its grid, sized on the host.
@@ -161,12 +163,29 @@ struct qses_context {
     void tick(int k);                 // closes timeline interval k at "now"
     std::chrono::steady_clock::time_point tl_last;
 
+    // per-slice vertex and triangle counts of the last call in the reference's slicing mode
+    std::vector<unsigned> slice_nv, slice_nt;
+
     int fail(int code, const char *what, cudaError_t e = cudaSuccess);
     void mark(const char *name);
 };
 
 namespace qses {
+// Bounds of the device atoms (one read-back) and the molecule's grid, into ctx->grid.
+int molecule_grid(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n, QGrid &g,
+                  bool sliced);
 int run_pipeline(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n);
+// The reference's slicing (QSES_FLAG_REFERENCE_SLICES): slice after slice of p.slice voxels,
+// each meshed, welded and smoothed alone; the meshes concatenated on the host as
+// API_computeSES does (vertex ids offset by the vertices of earlier slices).
+struct SlicedMesh {
+    std::vector<float> vertices;              // 3 per vertex
+    std::vector<int> triangles;               // 3 per triangle (kept, or all with keep_all)
+    std::vector<int> atom_sorted, atom_input;
+    std::vector<unsigned> slice_nv, slice_nt;  // per slice with a mesh, in slice order
+};
+int run_pipeline_slices(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n,
+                        SlicedMesh &out);
 // `passes` exact Gauss-Seidel passes over vertices [0, nv): positions vq (3 floats each) in
 // and out, CSR (deg offsets, nbr), shape sh.  The vertices run in sequential waves of at
 // most the slab kernel's capacity; every dependency points to a lower id, so a wave only

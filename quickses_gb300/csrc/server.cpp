@@ -167,6 +167,7 @@ QSES_API int qses_server_submit(qses_server *s, const qses_request *req, unsigne
     if (!(req->voxel > 0.0f) || req->smooth_passes < 0 || req->smooth_passes > 1000 ||
         (req->n > 0 && (!req->atoms || !req->radii)))
         return QSES_ERR_INVALID_ARG;
+    if (req->flags & QSES_FLAG_REFERENCE_SLICES) return QSES_ERR_UNSUPPORTED;  // qses_compute only
     std::unique_ptr<Job> j(new Job());
     j->xyz.assign((const float *)req->atoms, (const float *)req->atoms + 3ull * req->n);
     j->r.assign(req->radii, req->radii + req->n);

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import quickses_gb300 as q
+import ref_slices
 
 pytestmark = pytest.mark.gpu
 
@@ -48,3 +49,35 @@ def test_field_matches_reference_kernels(ctx, case):
     inner = (slice(0, g.G - 1),) * 3
     assert np.abs(mine[inner] - ref[inner]).max() < 2e-6
     assert int(((mine < 0) != (ref < 0)).sum()) == 0
+
+
+REFSLICES = ref_slices.load()
+
+
+@pytest.mark.skipif(REFSLICES is None, reason="tests/golden/ref_slices.npz not generated")
+@pytest.mark.parametrize("case", ref_slices.cases(REFSLICES) if REFSLICES is not None else [])
+def test_slices_match_reference_build(ctx, case):
+    """The reference's slicing mode (QSES_FLAG_REFERENCE_SLICES) against the reference's own
+    per-slice meshes: the same slices with a mesh, each with the reference's vertices at the
+    same quantised positions (a rounding tie may put one a quantum apart), its triangles in
+    its order (degenerate ones kept, as the reference's slices hold them) and its sorted
+    closest-atom ids, once the never-written last triangle is set aside."""
+    xyz, rad, dx, sl = ref_slices.case_inputs(REFSLICES, case)
+    ref = ref_slices.slices(REFSLICES, case, 0)
+    m = ctx.compute(xyz, rad, voxel=dx, smooth=0, keep_degenerate=True, slice=sl, reference_slices=True)
+    counts = ctx.slice_counts()
+    assert len(counts) == len(ref)
+    v0 = t0 = near_total = total = 0
+    for k, (v, t, a) in enumerate(ref):
+        v, t, a = ref_slices.without_unwritten(v, t, a)
+        nv, nt = counts[k]
+        mv, mt = m.vertices[v0:v0 + nv], m.triangles[t0:t0 + nt] - v0
+        exact, near, unmatched, bad_tri = ref_slices.match(v, t, mv, mt)
+        assert unmatched == 0 and bad_tri == 0, (k, exact, near, unmatched, bad_tri)
+        if near == 0:
+            assert np.array_equal(a, m.atom_sorted[v0:v0 + nv])
+        near_total += near
+        total += nv
+        v0 += nv
+        t0 += nt
+    assert near_total <= max(2, total // 2000)

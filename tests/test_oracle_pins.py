@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 import quickses_gb300 as q
+import ref_slices
 from oracle import oracle as O
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -172,3 +173,47 @@ def test_oracle_matches_reference_cuda_build(case):
     assert (to_ref >= 0).all()
     # the reference never writes its last triangle and leaves a zero vertex instead
     assert np.array_equal(to_ref[m.triangles_kept[:len(tr)]], tr) and len(m.triangles_kept) == len(tr) + 1
+
+
+REFSLICES = ref_slices.load()
+
+
+@pytest.mark.skipif(REFSLICES is None, reason="tests/golden/ref_slices.npz not generated")
+@pytest.mark.parametrize("case", ref_slices.cases(REFSLICES) if REFSLICES is not None else [])
+def test_oracle_slices_match_reference_build(case):
+    """The oracle's restatement of the reference's slicing against the reference's own
+    per-slice meshes (computeSlicedSES with small SLICE values, several slices per axis):
+    the same slices, vertex and triangle counts per slice, every vertex at the same
+    quantised position (a rounding tie may put one a quantum apart) and the same triangles."""
+    xyz, rad, dx, sl = ref_slices.case_inputs(REFSLICES, case)
+    ref = ref_slices.slices(REFSLICES, case, 0)
+    m = O.compute_ses_slices(xyz, rad, dx, sl, smooth=0)
+    assert len(ref) == len(m.slice_v) - 1 and len(ref) > 8
+    near_total = total = 0
+    for k, (v, t, a) in enumerate(ref):
+        v, t, a = ref_slices.without_unwritten(v, t, a)
+        mv = m.vertices[m.slice_v[k]:m.slice_v[k + 1]].astype(np.float32)
+        mt = m.triangles[m.slice_t[k]:m.slice_t[k + 1]] - m.slice_v[k]
+        exact, near, unmatched, bad_tri = ref_slices.match(v, t, mv, mt)
+        assert unmatched == 0 and bad_tri == 0, (k, exact, near, unmatched, bad_tri)
+        near_total += near
+        total += len(v)
+    assert near_total <= max(2, total // 2000)  # rounding ties only
+
+
+@pytest.mark.skipif(REFSLICES is None, reason="tests/golden/ref_slices.npz not generated")
+@pytest.mark.parametrize("case", [c for c in (ref_slices.cases(REFSLICES) if REFSLICES is not None else [])
+                                  if ref_slices.slices(REFSLICES, c, 1) is not None])
+def test_reference_slice_smoothing_is_smoothmesh_of_its_slice(case):
+    """Each smoothed reference slice is the sequential Gauss-Seidel pass (the oracle's,
+    pinned to SmoothMesh.cpp) of that slice's own unsmoothed mesh, its unwritten last
+    triangle included: the only smoothing difference from this library's slices is that
+    triangle, whose corners hold stale device memory."""
+    p0 = ref_slices.slices(REFSLICES, case, 0)
+    p1 = ref_slices.slices(REFSLICES, case, 1)
+    assert len(p0) == len(p1)
+    for k, ((v0, t0, _), (v1, t1, _)) in enumerate(zip(p0, p1)):
+        assert len(v0) == len(v1) and np.array_equal(t0[:-1], t1[:-1])
+        sm = O.smooth_f32(v0, t1, 1)
+        real = ~np.isnan(v1).any(axis=1)
+        assert np.array_equal(sm[real], v1[real]), k
