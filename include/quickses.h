@@ -57,7 +57,10 @@ enum {
  * stay in library-owned buffers reachable through API_get*.  Triangles with a repeated
  * vertex index are dropped.  doSmoothing = number of Laplacian passes.  N <= 1 gives an
  * empty mesh.  Unlike the reference, a failure does not exit(): counts are left at 0 and
- * qses_api_last_status() reports the code. */
+ * qses_api_last_status() reports the code.  The mesh is the reference's output for one slice
+ * covering the grid; with the environment variable QSES_REFERENCE_SLICES set to a slice size
+ * (the reference's library uses 300) it is the reference's sliced output instead
+ * (QSES_FLAG_REFERENCE_SLICES). */
 QSES_API void API_computeSES(float resoSES, qses_float3 *atomPos, float *atomRad, unsigned int N,
                              qses_float3 *out_vertices, unsigned int *NVert, int *out_triangles,
                              unsigned int *NTri, int doSmoothing);

@@ -919,6 +919,15 @@ QSES_API void API_computeSES(float resoSES, qses_float3 *atomPos, float *atomRad
     qses_params_default(&p);
     p.voxel = resoSES;
     p.smooth_passes = doSmoothing < 0 ? 0 : doSmoothing;
+    // QSES_REFERENCE_SLICES=<slice voxels>: the reference's sliced output, as its library
+    // computes it with SLICE = 300 (CudaSurf.cu:63, 629-754)
+    if (const char *env = getenv("QSES_REFERENCE_SLICES")) {
+        const long sl = strtol(env, nullptr, 10);
+        if (sl > 0) {
+            p.slice = (int)std::min(sl, 1l << 20);
+            p.flags |= QSES_FLAG_REFERENCE_SLICES;
+        }
+    }
     qses_mesh m;
     g_api_status = qses_compute(g_api_ctx, &p, atomPos, atomRad, N, &m);
     if (g_api_status != QSES_OK) {

@@ -2,8 +2,11 @@
 //   QuickSES -i input.pdb -o output.obj [-l passes=1] [-v voxel=0.5] [-s slice=300] [-h]
 // -i and -o are mandatory; a missing one prints the usage and exits with -1, like the
 // reference's argument validation.  Degenerate triangles are kept, as the reference's OBJ
-// path keeps them.  -s is accepted for compatibility; the mesh does not depend on it.
-// Extra: -d device (default 0) and -t (print stage times to stderr).
+// path keeps them.  By default the mesh is the reference's single-slice result whatever -s
+// is; with -r it is the reference's sliced output for slices of -s voxels (each slice
+// meshed, welded and smoothed on its own, the OBJ holding the slices one after the other,
+// CudaSurf.cu:329-371, 629-754).
+// Extra: -r (the reference's slicing), -d device (default 0), -t (stage times to stderr).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -22,8 +25,9 @@ void usage(const char *prog) {
             "      -o[output.obj]                    Output OBJ mesh file\n"
             "      -l[smooth factor]                 (1) Times to run Laplacian smoothing step.\n"
             "      -v[voxel size]                    (0.5) Voxel size in Angstrom. Defines the quality of the mesh.\n"
-            "      -s[slice size]                    (300) Size of the sub-grid (accepted; the mesh does not\n"
-            "                                        depend on it).\n"
+            "      -s[slice size]                    (300) Size of the sub-grid (used with -r).\n"
+            "      -r                                The reference's slicing: one mesh per sub-grid of -s\n"
+            "                                        voxels, as QuickSES writes it.\n"
             "      -d[device]                        (0) CUDA device.\n"
             "      -t                                Print per-stage device times.\n"
             "      -h, --help                        Display this help menu\n",
@@ -64,7 +68,7 @@ int main(int argc, const char **argv) {
     std::string in, out;
     int passes = 1, slice = 300, device = 0;
     float voxel = 0.5f;
-    bool times = false;
+    bool times = false, slices = false;
     for (int k = 1; k < argc; k++) {
         const char *a = argv[k];
         if (!strcmp(a, "-h") || !strcmp(a, "--help")) {
@@ -80,6 +84,10 @@ int main(int argc, const char **argv) {
         const char f = a[1];
         if (f == 't' && !a[2]) {
             times = true;
+            continue;
+        }
+        if (f == 'r' && !a[2]) {
+            slices = true;
             continue;
         }
         if (!strchr("iolvsd", f) || !take_value(argc, argv, k, val)) {
@@ -107,6 +115,10 @@ int main(int argc, const char **argv) {
         usage(argv[0]);
         return -1;
     }
+    if (slices && slice < 1) {  // the reference would loop forever (CudaSurf.cu:653)
+        fprintf(stderr, "Argument '-s' must be at least 1 with -r\n");
+        return -1;
+    }
 
     float *xyz = nullptr, *rad = nullptr;
     unsigned n = 0;
@@ -128,7 +140,7 @@ int main(int argc, const char **argv) {
     p.voxel = voxel;
     p.smooth_passes = passes < 0 ? 0 : passes;
     p.slice = slice;
-    p.flags = QSES_FLAG_KEEP_DEGENERATE;
+    p.flags = QSES_FLAG_KEEP_DEGENERATE | (slices ? QSES_FLAG_REFERENCE_SLICES : 0);
     qses_mesh m;
     rc = qses_compute(ctx, &p, (const qses_float3 *)xyz, rad, n, &m);
     if (rc != QSES_OK) {

@@ -36,3 +36,22 @@ def test_cli_obj_matches_oracle(tmp_path, voxel, passes):
     ref = O.compute_ses(pxyz, prad, voxel, smooth=passes, fp64=False)
     # the OBJ path keeps degenerate triangles (CudaSurf.cu:363-368 writes every triangle)
     assert obj.read_text() == _expected_obj(ref.vertices.astype(np.float32), ref.triangles)
+
+
+def test_cli_reference_slices_obj_matches_oracle(tmp_path):
+    """-r -s 20: the reference's sliced output (one mesh per slice, concatenated), written
+    byte for byte as the oracle's restatement of that slicing gives it."""
+    xyz, _, el = q.molecules.ball(300, seed=18)
+    names = [chr(int(c)) for c in el]
+    pdb, obj = tmp_path / "m.pdb", tmp_path / "m.obj"
+    _write_pdb(pdb, xyz, names)
+    r = subprocess.run([CLI, "-i", str(pdb), "-o", str(obj), "-l", "1", "-v", "0.5", "-s", "20", "-r"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    pxyz, prad = q.read_pdb(pdb)
+    ref = O.compute_ses_slices(pxyz, prad, 0.5, 20, smooth=1)
+    assert len(ref.slice_v) > 2
+    assert obj.read_text() == _expected_obj(ref.vertices.astype(np.float32), ref.triangles)
+    bad = subprocess.run([CLI, "-i", str(pdb), "-o", str(obj), "-s", "0", "-r"], capture_output=True, text=True,
+                         timeout=60)
+    assert bad.returncode != 0

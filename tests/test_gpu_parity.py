@@ -160,3 +160,22 @@ def test_reference_api_semantics():
     assert np.array_equal(order[api.getAtomIdPerVert(nv)], ref.atom_input)
     api.freeMesh()
     assert api.exported_counts() == (0, 0)
+
+
+def test_reference_api_with_reference_slices(monkeypatch):
+    """API_computeSES with QSES_REFERENCE_SLICES set: the reference's sliced output, its
+    concatenation and degenerate filter (CudaSurf.cu:796-836)."""
+    xyz, rad = _atoms("ball", 250, 3)
+    monkeypatch.setenv("QSES_REFERENCE_SLICES", "18")
+    api = q.ReferenceAPI()
+    nv, nidx = api.computeSES(0.5, xyz, rad, smooth=1)
+    ref = O.compute_ses_slices(xyz, rad, 0.5, 18, smooth=1)
+    assert len(ref.slice_v) > 2
+    assert nv == len(ref.vertices) and nidx == 3 * len(ref.triangles_kept)
+    assert np.array_equal(api.getVertices(nv), ref.vertices.astype(np.float32))
+    assert np.array_equal(api.getTriangles(nidx).reshape(-1, 3), ref.triangles_kept)
+    api.freeMesh()
+    monkeypatch.delenv("QSES_REFERENCE_SLICES")
+    nv, nidx = api.computeSES(0.5, xyz, rad, smooth=1)
+    assert nv == len(O.compute_ses(xyz, rad, 0.5, smooth=1).vertices)
+    api.freeMesh()
