@@ -134,7 +134,10 @@ QSES_API int qses_context_create(int device, void *cuda_stream, qses_context **o
 QSES_API int qses_context_destroy(qses_context *ctx);
 QSES_API void qses_params_default(qses_params *p);
 
-/* Host atoms in, host mesh out (pinned, owned by *out until qses_mesh_release). */
+/* Host atoms in, host mesh out (pinned, owned by *out until qses_mesh_release).  A grid too
+ * large for one pass (more than 4096 voxels, or 2000 A, per axis) gets the reference's
+ * sliced output for p->slice (QSES_FLAG_REFERENCE_SLICES), as the reference slices every
+ * grid; qses_last_slices then reports its slices. */
 QSES_API int qses_compute(qses_context *ctx, const qses_params *p, const qses_float3 *atoms,
                           const float *radii, unsigned n, qses_mesh *out);
 QSES_API void qses_mesh_release(qses_mesh *m);

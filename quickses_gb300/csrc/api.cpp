@@ -342,6 +342,18 @@ QSES_API int qses_compute(qses_context *ctx, const qses_params *p, const qses_fl
     rc = qses::run_pipeline(ctx, *p, d_xyz, d_r, n);
     qses::HostDownload dl = ctx->dl;
     ctx->dl = qses::HostDownload();
+    if (rc == QSES_ERR_UNSUPPORTED && ctx->oversize && !dl.block) {
+        // A grid too large for one pass (more than 4096 voxels or 2000 A per axis): the
+        // reference slices every grid, so it gets the reference's sliced output
+        // (CudaSurf.cu:629-754), computed one slice box at a time.
+        qses_params ps = *p;
+        if (ps.slice < 1) ps.slice = 300;
+        ps.flags |= QSES_FLAG_REFERENCE_SLICES;
+        qses::SlicedMesh sm;
+        rc = qses::run_pipeline_slices(ctx, ps, d_xyz, d_r, n, sm);
+        if (rc) return rc;
+        return host_mesh_from_slices(ctx, sm, out);
+    }
     if (rc) {
         if (dl.block) {  // copies into it may still be queued
             cudaStreamSynchronize(ctx->stream);

@@ -622,6 +622,7 @@ static int enqueue_finish(qses_context *ctx, const FinishSeg &c, SegOut &o) {
 int molecule_grid(qses_context *ctx, const qses_params &p, const float *d_xyz, const float *d_r, unsigned n, QGrid &g,
                   bool sliced) {
     cudaStream_t s = ctx->stream;
+    ctx->oversize = false;
     unsigned *d_mm = (unsigned *)ctx->small;
     int *d_err = (int *)((char *)ctx->small + 64);
     QCHK(cudaMemsetAsync(d_mm, 0xff, 3 * sizeof(unsigned), s));  // min encodings start high
@@ -643,6 +644,11 @@ int molecule_grid(qses_context *ctx, const qses_params &p, const float *d_xyz, c
     float maxR = dec(h_mm[6]);
     std::string why;
     int rc = grid_from_bounds(mn, mx, maxR, n, p.voxel, g, &ctx->info, &why, sliced);
+    if (rc == QSES_ERR_UNSUPPORTED && !sliced) {
+        // too large for one pass: note whether the reference's slicing could take it
+        QGrid gs;
+        ctx->oversize = grid_from_bounds(mn, mx, maxR, n, p.voxel, gs, nullptr, nullptr, true) == QSES_OK;
+    }
     if (rc != QSES_OK) return ctx->fail(rc, why.c_str());
     ctx->grid = g;
     ctx->have_grid = true;

@@ -165,6 +165,8 @@ struct qses_context {
 
     // per-slice vertex and triangle counts of the last call in the reference's slicing mode
     std::vector<unsigned> slice_nv, slice_nt;
+    // the last call's grid was too large for one pass but fits the reference's slicing
+    bool oversize = false;
 
     int fail(int code, const char *what, cudaError_t e = cudaSuccess);
     void mark(const char *name);

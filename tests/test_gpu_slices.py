@@ -81,3 +81,24 @@ def test_slices_are_refused_where_they_do_not_apply(ctx):
     # the next plain call reports no slices
     ctx.compute(xyz, rad, voxel=0.5)
     assert ctx.slice_counts() == []
+
+
+def test_grid_too_large_for_one_pass_gets_the_reference_slicing(ctx):
+    """Two clusters 2 100 A apart: a 4 300-voxel grid, beyond one pass.  The reference slices
+    every grid, so the call returns its sliced output (300-voxel slices), the same as asking
+    for that mode, with a surface around each cluster."""
+    a_xyz, a_rad, _ = q.molecules.ball(200, 109)
+    xyz = np.concatenate([a_xyz, a_xyz + np.float32([2100.0, 0.0, 0.0])])
+    rad = np.concatenate([a_rad, a_rad])
+    with pytest.raises(q.QSESError):
+        q.grid_info(xyz, rad, 0.5)  # no single-pass grid
+    m = ctx.compute(xyz, rad, voxel=0.5, smooth=1)
+    counts = ctx.slice_counts()
+    assert len(counts) >= 2 and sum(c[0] for c in counts) == len(m.vertices)
+    s = ctx.compute(xyz, rad, voxel=0.5, smooth=1, slice=300, reference_slices=True)
+    assert np.array_equal(m.vertices, s.vertices) and np.array_equal(m.triangles, s.triangles)
+    near_a = m.vertices[:, 0] < 1000.0
+    assert near_a.any() and (~near_a).any()
+    # each cluster's surface: the far one is the near one moved by 2100 A, up to the slice
+    # seams that cut them differently
+    assert abs(int(near_a.sum()) - int((~near_a).sum())) < 0.2 * len(m.vertices)
