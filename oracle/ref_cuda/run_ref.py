@@ -204,11 +204,18 @@ def field(cases=((200, 61, 0.5), (300, 62, 0.4), (150, 63, 0.3), (120, 64, 0.2),
             print(json.dumps(res), flush=True)
 
 
+# Molecules of tests/golden/ref_cuda.npz: (atoms, seed, voxel).  c2 is the 1 000-atom
+# workload itself (85^3, one slice in the reference); c4 at 0.2 A holds the tie voxels where
+# the field is exactly zero in real arithmetic and the reference's fast-math sign is
+# arbitrary (code 49: 1.4 - 0.2 * 7).
+FIXTURE_CASES = [(80, 71, 0.5), (60, 72, 0.3), (1000, 1, 0.5), (300, 73, 0.4), (120, 74, 0.2)]
+
+
 def fixtures(out=os.path.join(ROOT, "tests", "golden", "ref_cuda.npz")):
     ref = Ref()
     data = {}
-    for ci, (n, seed, dx) in enumerate([(80, 71, 0.5), (60, 72, 0.3)]):
-        xyz, rad, _ = q.molecules.ball(n, seed)
+    for ci, (n, seed, dx) in enumerate(FIXTURE_CASES):
+        xyz, rad = O.synth_ball(n, seed)
         p = "c%d_" % ci
         data[p + "xyz"], data[p + "rad"], data[p + "dx"] = xyz, rad, np.float32(dx)
         data[p + "field"] = ref.field(xyz, rad, dx).astype(np.float32)
@@ -371,6 +378,6 @@ if __name__ == "__main__":
     elif mode == "field":
         field()
     elif mode == "fixtures":
-        fixtures()
+        fixtures(*sys.argv[2:3])
     elif mode == "slices":
         slices(*sys.argv[2:3])

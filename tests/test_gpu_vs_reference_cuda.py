@@ -16,7 +16,12 @@ import ref_slices
 pytestmark = pytest.mark.gpu
 
 GOLD = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_cuda.npz"))
-CASES = sorted({k.split("_")[0] for k in GOLD.files})
+ALL = sorted({k.split("_")[0] for k in GOLD.files})
+# Voxel sizes where probe / dx is a whole number of voxels (0.2 A: 7) have tie voxels whose
+# field is exactly zero in real arithmetic; the reference's fast-math sign there is
+# arbitrary, so those cases are compared by tie-aware tests.
+TIE = [c for c in ALL if abs(1.4 / float(GOLD[c + "_dx"]) - round(1.4 / float(GOLD[c + "_dx"]))) < 1e-4]
+CASES = [c for c in ALL if c not in TIE]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -37,18 +42,41 @@ def test_unsmoothed_mesh_matches_reference_build(ctx, case):
     assert np.array_equal(ar[mine_to_ref], m.atom_sorted)          # same sorted atom ids
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", ALL)
 def test_field_matches_reference_kernels(ctx, case):
-    """Voxel values against the reference's probeIntersection + distanceFieldRefine."""
+    """Voxel values against the reference's probeIntersection + distanceFieldRefine: within
+    2e-6 A everywhere, the same sign everywhere but at tie voxels (code (probe/dx)^2, value
+    exactly zero in real arithmetic), where the reference's sign is arbitrary."""
     from oracle import oracle as O
     xyz, rad, dx = GOLD[case + "_xyz"], GOLD[case + "_rad"], float(GOLD[case + "_dx"])
     g, _ = O.grid(xyz, rad, dx)
     ctx.compute(xyz, rad, voxel=dx, smooth=0)
-    mine = O.lut(g)[ctx.debug_codes(g.G)]
+    codes = ctx.debug_codes(g.G)
+    mine = O.lut(g)[codes]
     ref = GOLD[case + "_field"]
     inner = (slice(0, g.G - 1),) * 3
     assert np.abs(mine[inner] - ref[inner]).max() < 2e-6
-    assert int(((mine < 0) != (ref < 0)).sum()) == 0
+    flips = (mine < 0) != (ref < 0)
+    if case in TIE:
+        tie = round((1.4 / dx) ** 2)
+        assert (codes[flips] == tie).all() and 0 < int(flips.sum()) <= int((codes == tie).sum())
+    else:
+        assert int(flips.sum()) == 0
+
+
+@pytest.mark.parametrize("case", TIE)
+def test_tie_case_mesh_close_to_reference_build(ctx, case):
+    """0.2 A: the tie voxels' arbitrary signs change a few marching-cubes cases, not the
+    surface: the unsmoothed meshes are within 0.005 voxel (symmetric Hausdorff)."""
+    from oracle import oracle as O
+    xyz, rad, dx = GOLD[case + "_xyz"], GOLD[case + "_rad"], float(GOLD[case + "_dx"])
+    m = ctx.compute(xyz, rad, voxel=dx, smooth=0)
+    vr, tr = GOLD[case + "_v0"], GOLD[case + "_t0"]
+    used = np.zeros(len(vr), bool)
+    used[tr.ravel()] = True  # the reference's stray vertex of its unwritten triangle is left out
+    ids = np.cumsum(used) - 1
+    h, _, _ = O.hausdorff(m.vertices.astype(np.float64), m.triangles, vr[used].astype(np.float64), ids[tr])
+    assert h <= 0.005 * dx
 
 
 REFSLICES = ref_slices.load()

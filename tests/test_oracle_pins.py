@@ -154,19 +154,38 @@ def test_oracle_smoothing_is_sequential_gauss_seidel():
 REFCUDA = np.load(os.path.join(HERE, "golden", "ref_cuda.npz"))
 
 
+def _tie_code(dx):
+    """Code whose value is exactly zero in real arithmetic (probe/dx whole), else None."""
+    r = 1.4 / dx
+    return round(r * r) if abs(r - round(r)) < 1e-4 else None
+
+
 @pytest.mark.parametrize("case", sorted({k.split("_")[0] for k in REFCUDA.files}))
 def test_oracle_matches_reference_cuda_build(case):
     """Outputs of QuickSES's own CUDA build (oracle/ref_cuda/run_ref.py fixtures): its field
-    from probeIntersection + distanceFieldRefine, and its unsmoothed API_computeSES mesh."""
+    from probeIntersection + distanceFieldRefine, and its unsmoothed API_computeSES mesh.
+    At a tie voxel size (0.2 A) the reference's sign of an exactly-zero value is arbitrary:
+    flips are allowed there only, and the mesh is compared geometrically."""
     d = REFCUDA
     xyz, rad, dx = d[case + "_xyz"], d[case + "_rad"], float(d[case + "_dx"])
     g, _ = O.grid(xyz, rad, dx)
-    mine = O.lut(g)[O.field_codes(xyz, rad, g)]
+    codes = O.field_codes(xyz, rad, g)
+    mine = O.lut(g)[codes]
     ref = d[case + "_field"]
     inner = (slice(0, g.G - 1),) * 3
     assert np.abs(mine[inner] - ref[inner]).max() < 2e-6       # fast-math FP32 vs our FP32
-    assert int(((mine < 0) != (ref < 0)).sum()) == 0
+    flips = (mine < 0) != (ref < 0)
+    tie = _tie_code(dx)
     m = O.compute_ses(xyz, rad, dx, smooth=0)
+    if tie is not None:
+        assert (codes[flips] == tie).all()
+        vr, tr = d[case + "_v0"], d[case + "_t0"]
+        used = np.zeros(len(vr), bool)
+        used[tr.ravel()] = True
+        h, _, _ = O.hausdorff(m.vertices, m.triangles_kept, vr[used].astype(np.float64), (np.cumsum(used) - 1)[tr])
+        assert h <= 0.005 * dx
+        return
+    assert int(flips.sum()) == 0
     vr, tr = d[case + "_v0"], d[case + "_t0"]
     index = {tuple(p): i for i, p in enumerate(vr.tolist())}
     to_ref = np.array([index.get(tuple(p), -1) for p in m.vertices.astype(np.float32).tolist()])
