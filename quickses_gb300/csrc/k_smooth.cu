@@ -68,6 +68,10 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
     extern __shared__ unsigned s_dyn[];
     __shared__ unsigned s_head, s_tail, s_done, s_stop, s_ob_head, s_ob_tail, s_slab;
     __shared__ unsigned s_ob[kGsOutbox];
+    // Per worker warp: one row of neighbour positions, summed in list order by lane 0 (of
+    // each lane group): one shared-memory round trip, then a chain of adds in registers,
+    // instead of a shuffle per entry.
+    __shared__ float4 s_stage[kGsT / 32][32];
     unsigned *st = s_dyn;                                        // len + 1 CSR offsets of the slab
     unsigned *cnt = s_dyn + (smax + 1);                          // (len + 1) / 2 words: packed counters
     volatile unsigned short *ring = (volatile unsigned short *)(cnt + (smax + 1) / 2);  // slab offsets
@@ -255,23 +259,20 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
                         asm volatile("mov.b32 %0, %1;" : "=f"(t) : "f"(q.x));
                         cyc_pos += clock64() - ca + (t != t ? 1 : 0);
                     }
-                    // strictly in neighbour-list order; lanes past m add +0.0f (a sum that
-                    // started at +0.0f is unchanged by it)
-                    const float qx = lane < m ? q.x : 0.0f, qy = lane < m ? q.y : 0.0f, qz = lane < m ? q.z : 0.0f;
-#pragma unroll
-                    for (unsigned k = 0; k < 16; k++) {
-                        sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
-                        sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
-                        sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
-                    }
-                    if (m > 16) {
-#pragma unroll
-                        for (unsigned k = 16; k < 32; k++) {
-                            sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, qx, k));
-                            sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, qy, k));
-                            sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, qz, k));
+                    // strictly in neighbour-list order, by lane 0 from the warp's row
+                    float4 *row = s_stage[threadIdx.x >> 5];
+                    if (lane < m) row[lane] = q;
+                    __syncwarp();
+                    if (lane == 0) {
+#pragma unroll 4
+                        for (unsigned k = 0; k < m; k++) {
+                            const float4 p = row[k];
+                            sx = __fadd_rn(sx, p.x);
+                            sy = __fadd_rn(sy, p.y);
+                            sz = __fadd_rn(sz, p.z);
                         }
                     }
+                    __syncwarp();  // the row is rewritten by the next chunk or vertex
                 }
                 const float n = (float)(int)(e1 - e0);
                 if (lane == 0) {
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
 #pragma unroll
                 for (unsigned j = 0; j < 2; j++) {
                     // weak loads: the CTA- and GPU-scope acquires order them; lanes past the
-                    // list add +0.0f (a sum that started at +0.0f is unchanged by it)
+                    // list load nothing (their slots are not summed)
                     q[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     if (r0 + j * kLanes + gl < nlen) {
                         if (kSP && id[j] - a < len) q[j] = spos[id[j] - a];
@@ -429,15 +430,26 @@ __global__ void __launch_bounds__(kGsT, kGsT <= 512 ? 2 : 1) k_gs_flow(float4 *p
                     first_id[0] = id[0];
                     first_id[1] = id[1];
                 }
+                // strictly in neighbour-list order, by each group's lane 0 from the warp's row
+                // (a group's entries sit in its own kLanes slots)
+                float4 *row = s_stage[threadIdx.x >> 5];
 #pragma unroll
                 for (unsigned j = 0; j < 2; j++) {
                     if (r0 + j * kLanes >= maxlen) break;  // uniform: no group has entries here
-#pragma unroll
-                    for (unsigned k = 0; k < kLanes; k++) {  // strictly in neighbour-list order
-                        sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, q[j].x, k, kLanes));
-                        sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, q[j].y, k, kLanes));
-                        sz = __fadd_rn(sz, __shfl_sync(0xffffffffu, q[j].z, k, kLanes));
+                    row[lane] = q[j];
+                    __syncwarp();
+                    const unsigned o0 = r0 + j * kLanes;
+                    if (gl == 0 && o0 < nlen) {
+                        const unsigned cj = min(kLanes, nlen - o0);
+#pragma unroll 4
+                        for (unsigned k = 0; k < cj; k++) {
+                            const float4 p = row[g0 + k];
+                            sx = __fadd_rn(sx, p.x);
+                            sy = __fadd_rn(sy, p.y);
+                            sz = __fadd_rn(sz, p.z);
+                        }
                     }
+                    __syncwarp();  // the row is rewritten by the next chunk or vertex
                 }
             }
             if (act && gl == 0) {
