@@ -238,33 +238,38 @@ constexpr int kEdtNT = 256;
 // output rows) at the cost of shared memory (dynamic, edt_smem_bytes); the shape is chosen
 // by the autotuner.
 
-template <int TX, int TY>
-struct EdtSmem {
-    static constexpr int HXM = TX + 2 * QSES_RMAX, HYM = TY + 2 * QSES_RMAX;
-    static constexpr size_t out_off = 0;                                          // [HXM HYM][3] words
-    static constexpr size_t g_off = (out_off + 12ull * HXM * HYM + 15) & ~15ull;  // [HXM HYM][32] bytes
-    static constexpr size_t h_off = g_off + 32ull * HXM * HYM;                    // [HXM][TY][32] bytes
-    static constexpr size_t in_off = h_off + 32ull * HXM * TY;                    // [TX TY] words
-    static constexpr size_t ot_off = in_off + 4ull * TX * TY;                     // [TX TY] words
-    static constexpr size_t bytes = ot_off + 4ull * TX * TY;
+// Shared-memory layout of one refine tile for a window of R voxels: the halo rows' outside
+// words (only without precomputed z distances), their z distances, the y-pass rows, and the
+// tile's in/out words.  Sized per launch, so a smaller window (a larger voxel) fits more CTAs
+// per SM; the largest layout (R = QSES_RMAX, no z distances) bounds every other.
+struct EdtLayout {
+    size_t g_off, h_off, in_off, ot_off, bytes;
 };
+__host__ __device__ __forceinline__ EdtLayout edt_layout(int TX, int TY, int R, bool have_zd) {
+    const size_t HX = (size_t)TX + 2 * R, HY = (size_t)TY + 2 * R;
+    EdtLayout L;
+    L.g_off = have_zd ? 0 : ((12 * HX * HY + 15) & ~(size_t)15);  // [HX HY][3] outside words first
+    L.h_off = L.g_off + 32 * HX * HY;                                 // [HX HY][32] z distances
+    L.in_off = L.h_off + 32 * HX * (size_t)TY;                         // [HX][TY][32] y-pass rows
+    L.ot_off = L.in_off + 4 * (size_t)TX * TY;
+    L.bytes = L.ot_off + 4 * (size_t)TX * TY;
+    return L;
+}
 
 template <int TX, int TY>
 __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, const unsigned *__restrict__ inMask,
                                          const unsigned *__restrict__ outMask, unsigned char *__restrict__ codes,
                                          unsigned *__restrict__ signMask,
                                          const unsigned char *__restrict__ zd = nullptr) {
-    using L = EdtSmem<TX, TY>;
-    constexpr int HYM = L::HYM;
+    const EdtLayout L = edt_layout(TX, TY, g.R, zd != nullptr);
     extern __shared__ __align__(16) unsigned char edt_smem[];
-    unsigned (*s_out)[3] = reinterpret_cast<unsigned (*)[3]>(edt_smem + L::out_off);
+    unsigned (*s_out)[3] = reinterpret_cast<unsigned (*)[3]>(edt_smem);  // without zd only
     // Squared distances, one byte per voxel (255 = none); the y and x passes work on four
     // voxels per 32-bit word with saturating byte adds, so 255 stays "none".
-    unsigned char (*s_g)[32] = reinterpret_cast<unsigned char (*)[32]>(edt_smem + L::g_off);
-    unsigned char (*s_h)[TY][32] = reinterpret_cast<unsigned char (*)[TY][32]>(edt_smem + L::h_off);
-    unsigned *s_in = reinterpret_cast<unsigned *>(edt_smem + L::in_off);
-    unsigned *s_ot = reinterpret_cast<unsigned *>(edt_smem + L::ot_off);
-    (void)HYM;
+    unsigned char (*s_g)[32] = reinterpret_cast<unsigned char (*)[32]>(edt_smem + L.g_off);
+    unsigned char (*s_h)[TY][32] = reinterpret_cast<unsigned char (*)[TY][32]>(edt_smem + L.h_off);
+    unsigned *s_in = reinterpret_cast<unsigned *>(edt_smem + L.in_off);
+    unsigned *s_ot = reinterpret_cast<unsigned *>(edt_smem + L.ot_off);
     const int j0 = jb * TY, i0 = ib * TX;
     const int R = g.R, G = g.G, W = g.W, t = threadIdx.x;
     const int HX = TX + 2 * R, HY = TY + 2 * R, k0 = w * 32;
@@ -525,12 +530,12 @@ void launch_sas(const QGrid &g, const float4 *atoms, const uint2 *cells, unsigne
 template <int TX, int TY>
 static void launch_edt_shape(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
                              unsigned *signMask, cudaStream_t s, const unsigned char *zd) {
-    constexpr size_t smem = EdtSmem<TX, TY>::bytes;
     static const bool attr = [] {
         return cudaFuncSetAttribute((const void *)k_edt<TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem) == cudaSuccess;
+                                    (int)edt_layout(TX, TY, QSES_RMAX, false).bytes) == cudaSuccess;
     }();
     (void)attr;
+    const size_t smem = edt_layout(TX, TY, g.R, zd != nullptr).bytes;
     dim3 grid(g.W, (g.G + TY - 1) / TY, (g.G + TX - 1) / TX);
     k_edt<TX, TY><<<grid, kEdtNT, smem, s>>>(g, inMask, outMask, codes, signMask, zd);
 }
@@ -542,8 +547,8 @@ void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask,
         const size_t words = (size_t)g.G * g.G * g.W;
         k_edt_z<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(g, outMask, zd);
     }
-    // shape 0: 8 x 8 rows (37 KB of shared memory), 1: 16 x 8 (48 KB), 2: 16 x 16 (66 KB),
-    // 3: 32 x 16 (99 KB)
+    // shape 0: 8 x 8 rows, 1: 16 x 8, 2: 16 x 16, 3: 32 x 16 (shared memory per CTA at R = 7
+    // with z distances: 21, 29, 45 and 70 KB)
     switch (shape) {
         case 3: launch_edt_shape<32, 16>(g, inMask, outMask, codes, signMask, s, zd); break;
         case 2: launch_edt_shape<16, 16>(g, inMask, outMask, codes, signMask, s, zd); break;
@@ -568,7 +573,7 @@ void launch_edt_batch(const QBatch &b, unsigned tiles, const unsigned *inMask, c
                       unsigned char *codes, unsigned *signMask, unsigned *counter, cudaStream_t s, unsigned words,
                       unsigned char *zd) {
     if (zd) k_edt_z_batch<<<(words + 255) / 256, 256, 0, s>>>(b, words, outMask, zd);
-    constexpr size_t smem = EdtSmem<8, 8>::bytes;
+    const size_t smem = edt_layout(8, 8, QSES_RMAX, false).bytes;  // molecules of any window
     k_edt_batch<<<persistent_blocks((const void *)k_edt_batch, kEdtNT, tiles, smem), kEdtNT, smem, s>>>(
         b, inMask, outMask, codes, signMask, counter, zd);
 }
