@@ -706,9 +706,10 @@ double pt_tri_d2(V3 p, V3 a, V3 b, V3 c) {
     return dot(d, d);
 }
 
-/* max over vertices of A of the distance to surface B */
+/* max over vertices of A (those with only[v] set, when only is given) of the distance to
+   surface B */
 double one_sided(const double *va, unsigned nva, const double *vb, unsigned nvb, const int32_t *tb,
-                 unsigned ntb, double *per_vertex = nullptr) {
+                 unsigned ntb, double *per_vertex = nullptr, const uint8_t *only = nullptr) {
     if (nva == 0 || ntb == 0) return nva == 0 ? 0.0 : std::numeric_limits<double>::infinity();
     double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
     double elen = 0;
@@ -741,6 +742,7 @@ double one_sided(const double *va, unsigned nva, const double *vb, unsigned nvb,
     double worst = 0;
 #pragma omp parallel for schedule(dynamic, 256) reduction(max : worst)
     for (int64_t v = 0; v < (int64_t)nva; v++) {
+        if (only && !only[v]) continue;
         V3 p = {va[3 * v], va[3 * v + 1], va[3 * v + 2]};
         int b0[3] = {binof(p.x, 0), binof(p.y, 1), binof(p.z, 2)};
         double best = std::numeric_limits<double>::infinity();
@@ -900,8 +902,13 @@ void oracle_smooth_f32(float *v, unsigned nv, const int32_t *tri, unsigned nt, i
 double oracle_hausdorff(const double *va, unsigned nva, const int32_t *ta, unsigned nta, const double *vb,
                         unsigned nvb, const int32_t *tb, unsigned ntb, double *ab, double *ba, int nthreads) {
     set_threads(nthreads);
-    double x = one_sided(va, nva, vb, nvb, tb, ntb);
-    double y = one_sided(vb, nvb, va, nva, ta, nta);
+    /* Surface to surface: a vertex that no triangle names (one left only by degenerate,
+       filtered triangles) is not on either surface and is not measured. */
+    std::vector<uint8_t> ua(nva, 0), ub(nvb, 0);
+    for (unsigned i = 0; i < 3 * nta; i++) ua[ta[i]] = 1;
+    for (unsigned i = 0; i < 3 * ntb; i++) ub[tb[i]] = 1;
+    double x = one_sided(va, nva, vb, nvb, tb, ntb, nullptr, ua.data());
+    double y = one_sided(vb, nvb, va, nva, ta, nta, nullptr, ub.data());
     if (ab) *ab = x;
     if (ba) *ba = y;
     return std::max(x, y);

@@ -179,3 +179,26 @@ def test_reference_api_with_reference_slices(monkeypatch):
     nv, nidx = api.computeSES(0.5, xyz, rad, smooth=1)
     assert nv == len(O.compute_ses(xyz, rad, 0.5, smooth=1).vertices)
     api.freeMesh()
+
+
+@pytest.mark.parametrize("n,dx,passes", [(20000, 0.2, 1), (5000, 0.4, 2)])
+def test_mesh_vs_fp64_at_scale(ctx, n, dx, passes):
+    """The FP32 GPU mesh against the FP64 oracle on large molecules (20 000 atoms at 0.2 A:
+    1.7 M vertices; 5 000 atoms at 0.4 A with two passes).  At this size a few voxels sit on
+    an FP32 rounding tie of the SAS test (|p - a|^2 against (r + probe)^2; 16 of 126 M voxels
+    on the 20 000-atom ball), where FP32 and FP64 classify them differently, as the
+    reference's FP32 kernel does.  Each such flip moves the surface near that voxel only:
+    symmetric Hausdorff within half a voxel, and under 1e-4 of the vertices farther than
+    0.05 voxel from the FP64 surface (measured: 0.25 voxel and 34 of 1 668 491)."""
+    xyz, rad, _ = q.molecules.ball(n, 1)
+    m = ctx.compute(xyz, rad, voxel=dx, smooth=passes)
+    ref = O.compute_ses(xyz, rad, dx, smooth=passes, fp64=True)
+    v = m.vertices.astype(np.float64)
+    h, _, _ = O.hausdorff(v, m.triangles, ref.vertices, ref.triangles_kept)
+    assert h <= 0.5 * dx, "Hausdorff %.4g A > %.4g A" % (h, 0.5 * dx)
+    used = np.zeros(len(v), bool)
+    used[m.triangles.ravel()] = True
+    d = O.point_surface(v[used], ref.vertices, ref.triangles_kept)
+    far = int((d > HAUSDORFF_TOL * dx).sum())
+    assert far <= 1e-4 * len(d), "%d of %d vertices farther than %.3g A" % (far, len(d), HAUSDORFF_TOL * dx)
+    assert abs(len(m.vertices) - len(ref.vertices)) <= max(2, 0.01 * len(ref.vertices))
