@@ -280,7 +280,9 @@ QSES_API unsigned long long qses_last_download_bytes(qses_context *ctx);
  * boundary polls of one slab, [3] slabs that did not finish, [4] clock cycles spent in
  * vertex updates, [5] in releasing successors, [6] vertices updated, [7] cycles until a
  * vertex's neighbour ids arrived, [8] then until their positions arrived, [9] in the
- * position store and its fence (summed over warps).  Returns the number of values written. */
+ * position store and its fence (summed over warps); [2]-[9] are counted on calls
+ * made with profiling on (qses_set_profiling) and are 0 otherwise.  Returns the number of
+ * values written. */
 QSES_API int qses_diagnostics(qses_context *ctx, unsigned long long *out, int max);
 
 /* Host timeline of the last pipeline run on ctx (ms; for a batch call, its last batch):
