@@ -238,6 +238,18 @@ constexpr int kEdtNT = 256;
 // output rows) at the cost of shared memory (dynamic, edt_smem_bytes); the shape is chosen
 // by the autotuner.
 
+// Min-plus on four byte distances of a word (255 = none) without the byte-SIMD add and
+// min, which this GPU runs as several instructions each: the bytes are spread over two
+// words of 16-bit halves (one byte permute each), where adding a square <= 81 cannot carry
+// (255 + 81 < 2^16) and the 16-bit min is one instruction; packing back clamps at 255.
+// Real distances stay below 255 (y <= 2 R^2 = 162, x <= 3 R^2 = 243) and "none" at or above
+// it, so the results equal the saturating byte arithmetic's.
+__device__ __forceinline__ unsigned spread_lo(unsigned w) { return __byte_perm(w, 0u, 0x4140); }  // bytes 0, 1
+__device__ __forceinline__ unsigned spread_hi(unsigned w) { return __byte_perm(w, 0u, 0x4342); }  // bytes 2, 3
+__device__ __forceinline__ unsigned pack_bytes(unsigned lo, unsigned hi) {
+    return __byte_perm(__vminu2(lo, 0x00ff00ffu), __vminu2(hi, 0x00ff00ffu), 0x6420);
+}
+
 // Shared-memory layout of one refine tile for a window of R voxels: the halo rows' outside
 // words (only without precomputed z distances), their z distances, the y-pass rows, and the
 // tile's in/out words.  Sized per launch, so a smaller window (a larger voxel) fits more CTAs
@@ -307,12 +319,14 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
             // y: min over dj of dj^2 + g^2 (<= 2 R^2 = 162 < 255), four voxels per word.
             for (int q = t; q < HX * TY * 8; q += kEdtNT) {
                 const int w4 = q & 7, y = (q >> 3) % TY, hx = (q >> 3) / TY;
-                unsigned best = 0xffffffffu;
+                unsigned lo = 0xffffffffu, hi = 0xffffffffu;
                 for (int dj = -R; dj <= R; dj++) {
                     const unsigned gw = reinterpret_cast<const unsigned *>(s_g[hx * HY + y + R + dj])[w4];
-                    best = __vminu4(best, __vaddus4(gw, (unsigned)(dj * dj) * 0x01010101u));
+                    const unsigned d2 = (unsigned)(dj * dj) * 0x00010001u;
+                    lo = __vminu2(lo, spread_lo(gw) + d2);
+                    hi = __vminu2(hi, spread_hi(gw) + d2);
                 }
-                reinterpret_cast<unsigned *>(s_h[hx][y])[w4] = best;
+                reinterpret_cast<unsigned *>(s_h[hx][y])[w4] = pack_bytes(lo, hi);
             }
             __syncthreads();
         }
@@ -352,12 +366,14 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
         // y: min over dj of dj^2 + g^2 (<= 2 R^2 = 162 < 255), four voxels per word.
         for (int q = t; q < HX * TY * 8; q += kEdtNT) {
             const int w4 = q & 7, y = (q >> 3) % TY, hx = (q >> 3) / TY;
-            unsigned best = 0xffffffffu;
+            unsigned lo = 0xffffffffu, hi = 0xffffffffu;
             for (int dj = -R; dj <= R; dj++) {
                 const unsigned gw = reinterpret_cast<const unsigned *>(s_g[hx * HY + y + R + dj])[w4];
-                best = __vminu4(best, __vaddus4(gw, (unsigned)(dj * dj) * 0x01010101u));
+                const unsigned d2 = (unsigned)(dj * dj) * 0x00010001u;
+                lo = __vminu2(lo, spread_lo(gw) + d2);
+                hi = __vminu2(hi, spread_hi(gw) + d2);
             }
-            reinterpret_cast<unsigned *>(s_h[hx][y])[w4] = best;
+            reinterpret_cast<unsigned *>(s_h[hx][y])[w4] = pack_bytes(lo, hi);
         }
         __syncthreads();
     }
@@ -371,12 +387,17 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
         // min over di of di^2 + h (<= 3 R^2 = 243 < 255) for this thread's 8 voxels
         unsigned bw0 = 0xffffffffu, bw1 = 0xffffffffu;
         if (has_out) {
+            unsigned l0 = 0xffffffffu, h0 = 0xffffffffu, l1 = 0xffffffffu, h1 = 0xffffffffu;
             for (int di = -R; di <= R; di++) {
-                const unsigned *hrow = reinterpret_cast<const unsigned *>(s_h[x + R + di][y]);
-                const unsigned d2 = (unsigned)(di * di) * 0x01010101u;
-                bw0 = __vminu4(bw0, __vaddus4(hrow[2 * part], d2));
-                bw1 = __vminu4(bw1, __vaddus4(hrow[2 * part + 1], d2));
+                const uint2 hw = reinterpret_cast<const uint2 *>(s_h[x + R + di][y])[part];
+                const unsigned d2 = (unsigned)(di * di) * 0x00010001u;
+                l0 = __vminu2(l0, spread_lo(hw.x) + d2);
+                h0 = __vminu2(h0, spread_hi(hw.x) + d2);
+                l1 = __vminu2(l1, spread_lo(hw.y) + d2);
+                h1 = __vminu2(h1, spread_hi(hw.y) + d2);
             }
+            bw0 = pack_bytes(l0, h0);
+            bw1 = pack_bytes(l1, h1);
         }
         unsigned long long packed = 0ull;
 #pragma unroll

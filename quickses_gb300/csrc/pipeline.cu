@@ -162,7 +162,9 @@ static int g_edt_tune[2][16];  // [tuned?][log2 G]
 int edt_shape(int G) {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     const int b = std::min(bits_for((unsigned)G), 15);
-    return g_edt_tune[0][b] ? g_edt_tune[1][b] : 0;
+    // untuned: 16 x 16 z-rows per tile on large grids (664^3: 1.05 ms against 1.21 ms for
+    // 8 x 8), 8 x 8 on small ones
+    return g_edt_tune[0][b] ? g_edt_tune[1][b] : G >= 256 ? 2 : 0;
 }
 
 void edt_shape_record(int G, int shape) {
