@@ -426,6 +426,11 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
 // z pass of the refine, once per voxel: squared distance (in voxels, <= R^2, 255 = none) to
 // the nearest outside voxel along the z row within the R window, one thread per 32-voxel
 // word (same values as the per-bit pass inside edt_tile).  zd has the codes' layout.
+// Bit-parallel: the outside set grows by one voxel per step (two funnel shifts over the
+// neighbouring words), and the voxels first covered at step k are at distance k.
+__device__ __forceinline__ unsigned nibble_bytes(unsigned nib) {  // 4 bits -> 0xff in each set bit's byte
+    return ((nib * 0x00204081u) & 0x01010101u) * 0xffu;           // copies at bits 0, 7, 14, 21: no carries
+}
 __device__ __forceinline__ void edt_z_word(const QGrid &g, size_t q, const unsigned *__restrict__ outMask,
                                            unsigned char *__restrict__ zd) {
     const size_t row = q / g.W;
@@ -434,24 +439,25 @@ __device__ __forceinline__ void edt_z_word(const QGrid &g, size_t q, const unsig
     const unsigned a = w > 0 ? __ldg(outMask + base + w - 1) : 0u, c = __ldg(outMask + base + w),
                    d = w + 1 < W ? __ldg(outMask + base + w + 1) : 0u;
     unsigned out[8];
-    if ((a | c | d) == 0u) {
+    if ((a | c | d) == 0u || c == 0xffffffffu) {  // no outside voxel within 32, or all outside
 #pragma unroll
-        for (int k = 0; k < 8; k++) out[k] = 0xffffffffu;
+        for (int k = 0; k < 8; k++) out[k] = c ? 0u : 0xffffffffu;
     } else {
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-            unsigned word = 0u;
+        for (int j = 0; j < 8; j++) out[j] = ~nibble_bytes((c >> (4 * j)) & 0xfu);  // outside: 0, else none
+        unsigned cov = c;  // voxels with an outside voxel within k
+        for (int k = 1; k <= R; k++) {
+            // bit b of the right funnel shift is voxel b + k, of the left one voxel b - k
+            const unsigned nc = cov | __funnelshift_r(c, d, k) | __funnelshift_l(a, c, k);
+            const unsigned nw = nc & ~cov;  // nearest outside voxel at distance k
+            cov = nc;
+            if (nw == 0u) continue;
+            const unsigned v = (unsigned)(k * k) * 0x01010101u;
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const int bit = 4 * k + e;
-                const unsigned long long up = (((unsigned long long)d << 32) | c) >> bit;
-                const int du = up ? (__ffsll((long long)up) - 1) : 1000;
-                const unsigned long long dn = (((unsigned long long)c << 32) | a) << (31 - bit);
-                const int dd = dn ? __clzll((long long)dn) : 1000;
-                const int m = min(du, dd);
-                word |= (m <= R ? (unsigned)(m * m) : 255u) << (8 * e);
+            for (int j = 0; j < 8; j++) {
+                const unsigned m = nibble_bytes((nw >> (4 * j)) & 0xfu);
+                out[j] = (out[j] & ~m) | (v & m);
             }
-            out[k] = word;
         }
     }
     uint4 *dst = reinterpret_cast<uint4 *>(zd + row * g.Gp + (size_t)w * 32);
