@@ -81,13 +81,21 @@ __device__ __forceinline__ unsigned span_bits(int a, int b) {  // bits a..b incl
     return m << a;
 }
 
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Voxels k in [k0, klim] of one z row whose squared distance to the atom is below t.
 // The set is an interval (the predicate is monotone in |k - k_atom|); its ends are
 // estimated in closed form and verified with the exact predicate, with a brute-force
-// fallback if the estimate does not verify.
-__device__ unsigned zmask(float az, float sxy, float t, int k0, int klim, float dx, float oz, float inv_dx) {
+// fallback if the estimate does not verify (so the estimate's square root need not be
+// correctly rounded: one approximate instruction).
+__device__ __forceinline__ unsigned zmask(float az, float sxy, float t, int k0, int klim, float dx, float oz,
+                                          float inv_dx) {
     float kcf = fminf(fmaxf((az - oz) * inv_dx, -1.0e6f), 1.0e6f);
-    float h = sqrtf(fmaxf(t - sxy, 0.0f)) * inv_dx;
+    float h = sqrt_approx(fmaxf(t - sxy, 0.0f)) * inv_dx;
     int lo = max(k0, (int)ceilf(kcf - h));
     int hi = min(klim, (int)floorf(kcf + h));
     if (lo <= hi) {
