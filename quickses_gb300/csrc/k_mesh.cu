@@ -326,20 +326,20 @@ __device__ __forceinline__ void mc_row(const QGrid &g, long long row, bool valid
 }
 
 // Resident CTAs per SM: the emit is latency-bound, so four CTAs (64 registers, a few spilled)
-// beat three for whole-warp rows (0.89 -> 0.82 ms on a 664^3 grid); the lane-group rows of
-// small grids keep three.
+// beat three: whole-warp rows 0.89 -> 0.82 ms on a 664^3 grid, 4-lane rows 0.780 -> 0.750 ms.
 template <bool EMIT, bool FULL>
-__global__ void __launch_bounds__(256, FULL ? 4 : 3) k_mc(QGrid g, const unsigned *__restrict__ sign,
+__global__ void __launch_bounds__(256, 4) k_mc(QGrid g, const unsigned *__restrict__ sign,
                                             const unsigned char *__restrict__ codes, const float *__restrict__ lut,
                                             uint2 *__restrict__ rowCount, const uint2 *__restrict__ rowBase,
-                                            unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey) {
+                                            unsigned *__restrict__ tri, unsigned long long *__restrict__ vkey,
+                                            int lanes) {
     __shared__ unsigned long long s_tab[256];
     __shared__ float s_lut[256];
     __shared__ unsigned s_rec[EMIT ? 8 * 32 * kRecW : 1];  // per warp: one record per lane
     s_tab[threadIdx.x] = c_mc[threadIdx.x];
     if (EMIT) s_lut[threadIdx.x] = lut[threadIdx.x];
     __syncthreads();
-    const int E = g.Gc + 1, Lg = FULL ? 32 : mc_lanes(g.Gc);
+    const int E = g.Gc + 1, Lg = FULL ? 32 : lanes;
     const long long first = ((long long)blockIdx.x * 8 + (threadIdx.x >> 5)) * (32 / Lg), nrow = (long long)E * E;
     if (first >= nrow) return;  // the whole warp
     const long long row = first + (threadIdx.x & 31) / Lg;
@@ -693,23 +693,34 @@ __global__ void k_from_float4(const float4 *__restrict__ v4, unsigned nv, float 
 static inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
 int mc_rows_per_warp(int Gc) { return 32 / mc_lanes(Gc); }
+// Lanes per row of the single-molecule count and emit (the per-row totals do not depend on
+// it, so the two may differ).  Narrow groups put more rows in flight per warp; measured on
+// GB300 (count / emit ms): 664^3 grid 0.248 / 0.821 with whole-warp rows, 0.127 / 0.780
+// with 2 / 4 lanes; 502^3 0.105 / 0.404 -> 0.074 / 0.370; 85^3 emit 0.029 -> 0.023 with 8.
+static int mc_lanes_for(int Gc, bool emit) {
+    const int Wc = (Gc + 32) / 32;
+    if (Wc >= 8) return emit ? 4 : 2;
+    return emit ? 8 : mc_lanes(Gc);
+}
 void launch_mc_count(const QGrid &g, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
     size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
-    if (mc_lanes(g.Gc) == 32)
+    const int L = mc_lanes_for(g.Gc, false);
+    if (L == 32)
         k_mc<false, true><<<nblk(rows, 8), 256, 0, s>>>(g, sign, nullptr, nullptr, rowCount, nullptr, nullptr,
-                                                         nullptr);
+                                                         nullptr, 32);
     else
-        k_mc<false, false><<<nblk(rows, 8 * mc_rows_per_warp(g.Gc)), 256, 0, s>>>(g, sign, nullptr, nullptr,
-                                                                                 rowCount, nullptr, nullptr, nullptr);
+        k_mc<false, false><<<nblk(rows, 8 * (32 / L)), 256, 0, s>>>(g, sign, nullptr, nullptr,
+                                                                    rowCount, nullptr, nullptr, nullptr, L);
 }
 void launch_mc_emit(const QGrid &g, const unsigned *sign, const unsigned char *codes, const float *lut,
                     const uint2 *rowBase, unsigned *tri, unsigned long long *vkey, cudaStream_t s) {
     size_t rows = (size_t)(g.Gc + 1) * (g.Gc + 1);
-    if (mc_lanes(g.Gc) == 32)
-        k_mc<true, true><<<nblk(rows, 8), 256, 0, s>>>(g, sign, codes, lut, nullptr, rowBase, tri, vkey);
+    const int L = mc_lanes_for(g.Gc, true);
+    if (L == 32)
+        k_mc<true, true><<<nblk(rows, 8), 256, 0, s>>>(g, sign, codes, lut, nullptr, rowBase, tri, vkey, 32);
     else
-        k_mc<true, false><<<nblk(rows, 8 * mc_rows_per_warp(g.Gc)), 256, 0, s>>>(g, sign, codes, lut, nullptr,
-                                                                                rowBase, tri, vkey);
+        k_mc<true, false><<<nblk(rows, 8 * (32 / L)), 256, 0, s>>>(g, sign, codes, lut, nullptr,
+                                                                   rowBase, tri, vkey, L);
 }
 void launch_mc_count_batch(const QBatch &b, unsigned units, const unsigned *sign, uint2 *rowCount, cudaStream_t s) {
     k_mc_batch<false><<<nblk(units, 8), 256, 0, s>>>(b, sign, nullptr, rowCount, nullptr, nullptr, nullptr);
