@@ -593,7 +593,9 @@ __global__ void k_csr_scatter(const unsigned *__restrict__ tri, size_t n3, uint2
     occ[start[v].x + k] = (unsigned)q;
 }
 
-__global__ void k_csr_sortfill(const unsigned *__restrict__ tri, unsigned *__restrict__ occ, size_t n3, unsigned nv,
+// 12 resident CTAs per SM (at most 42 registers) instead of 9: the kernel waits on scattered
+// triangle reads, so more warps in flight hide them
+__global__ void __launch_bounds__(128, 12) k_csr_sortfill(const unsigned *__restrict__ tri, unsigned *__restrict__ occ, size_t n3, unsigned nv,
                                uint2 *__restrict__ start, unsigned *__restrict__ nbr) {
     const unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v > nv) return;

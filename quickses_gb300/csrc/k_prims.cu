@@ -13,7 +13,9 @@
 namespace qses {
 
 // ------------------------------------------------------------------ scan
-constexpr int kScanT = 256, kScanI = 8, kScanTile = kScanT * kScanI;
+// 16 items per thread: half the tiles of 8, so a shorter look-back chain (neighbour-list
+// build 0.75 -> 0.71 ms on the 50 000-atom mesh, together with the sortfill's register cap)
+constexpr int kScanT = 256, kScanI = 16, kScanTile = kScanT * kScanI;
 
 __device__ __forceinline__ unsigned long long pack31(uint2 v) {
     return (unsigned long long)(v.x & 0x7fffffffu) | ((unsigned long long)(v.y & 0x7fffffffu) << 31);
