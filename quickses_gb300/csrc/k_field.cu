@@ -258,6 +258,37 @@ __device__ __forceinline__ unsigned pack_bytes(unsigned lo, unsigned hi) {
     return __byte_perm(__vminu2(lo, 0x00ff00ffu), __vminu2(hi, 0x00ff00ffu), 0x6420);
 }
 
+// Squared z distances of one 32-voxel word c (bit = outside voxel) with its neighbouring
+// words a (below) and d (above), one byte per voxel (<= R^2, 255 = none), four per output
+// word.  Bit-parallel: the outside set grows by one voxel per step (two funnel shifts over
+// the neighbouring words), and the voxels first covered at step k are at distance k.
+__device__ __forceinline__ unsigned nibble_bytes(unsigned nib) {  // 4 bits -> 0xff in each set bit's byte
+    return ((nib * 0x00204081u) & 0x01010101u) * 0xffu;           // copies at bits 0, 7, 14, 21: no carries
+}
+__device__ __forceinline__ void z_word(unsigned a, unsigned c, unsigned d, int R, unsigned out[8]) {
+    if ((a | c | d) == 0u || c == 0xffffffffu) {  // no outside voxel within 32, or all outside
+#pragma unroll
+        for (int k = 0; k < 8; k++) out[k] = c ? 0u : 0xffffffffu;
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) out[j] = ~nibble_bytes((c >> (4 * j)) & 0xfu);  // outside: 0, else none
+    unsigned cov = c;  // voxels with an outside voxel within k
+    for (int k = 1; k <= R; k++) {
+        // bit b of the right funnel shift is voxel b + k, of the left one voxel b - k
+        const unsigned nc = cov | __funnelshift_r(c, d, k) | __funnelshift_l(a, c, k);
+        const unsigned nw = nc & ~cov;  // nearest outside voxel at distance k
+        cov = nc;
+        if (nw == 0u) continue;
+        const unsigned v = (unsigned)(k * k) * 0x01010101u;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const unsigned m = nibble_bytes((nw >> (4 * j)) & 0xfu);
+            out[j] = (out[j] & ~m) | (v & m);
+        }
+    }
+}
+
 // Shared-memory layout of one refine tile for a window of R voxels: the halo rows' outside
 // words (only without precomputed z distances), their z distances, the y-pass rows, and the
 // tile's in/out words.  Sized per launch, so a smaller window (a larger voxel) fits more CTAs
@@ -355,20 +386,14 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
         has_out = __syncthreads_or(any);
     }
     if (has_border && has_out && !zd) {
-        // z: squared distance (in voxels, <= R^2) to the nearest outside voxel along the row.
-        for (int q = t; q < HX * HY * 32; q += kEdtNT) {
-            const int row = q >> 5, b = q & 31;
-            const unsigned a = s_out[row][0], c = s_out[row][1], d = s_out[row][2];
-            unsigned char gv = 255;
-            if (a | c | d) {
-                unsigned long long up = (((unsigned long long)d << 32) | c) >> b;
-                int du = up ? (__ffsll((long long)up) - 1) : 1000;
-                unsigned long long dn = (((unsigned long long)c << 32) | a) << (31 - b);
-                int dd = dn ? __clzll((long long)dn) : 1000;
-                int m = min(du, dd);
-                if (m <= R) gv = (unsigned char)(m * m);
-            }
-            s_g[row][b] = gv;
+        // z: squared distance (in voxels, <= R^2) to the nearest outside voxel along the row,
+        // one row of 32 voxels per thread
+        for (int q = t; q < HX * HY; q += kEdtNT) {
+            unsigned out[8];
+            z_word(s_out[q][0], s_out[q][1], s_out[q][2], R, out);
+            uint4 *dst = reinterpret_cast<uint4 *>(s_g[q]);
+            dst[0] = make_uint4(out[0], out[1], out[2], out[3]);
+            dst[1] = make_uint4(out[4], out[5], out[6], out[7]);
         }
         __syncthreads();
         // y: min over dj of dj^2 + g^2 (<= 2 R^2 = 162 < 255), four voxels per word.
@@ -433,41 +458,16 @@ __device__ __forceinline__ void edt_tile(const QGrid &g, int w, int jb, int ib, 
 
 // z pass of the refine, once per voxel: squared distance (in voxels, <= R^2, 255 = none) to
 // the nearest outside voxel along the z row within the R window, one thread per 32-voxel
-// word (same values as the per-bit pass inside edt_tile).  zd has the codes' layout.
-// Bit-parallel: the outside set grows by one voxel per step (two funnel shifts over the
-// neighbouring words), and the voxels first covered at step k are at distance k.
-__device__ __forceinline__ unsigned nibble_bytes(unsigned nib) {  // 4 bits -> 0xff in each set bit's byte
-    return ((nib * 0x00204081u) & 0x01010101u) * 0xffu;           // copies at bits 0, 7, 14, 21: no carries
-}
+// word.  zd has the codes' layout.
 __device__ __forceinline__ void edt_z_word(const QGrid &g, size_t q, const unsigned *__restrict__ outMask,
                                            unsigned char *__restrict__ zd) {
     const size_t row = q / g.W;
-    const int w = (int)(q - row * g.W), W = g.W, R = g.R;
+    const int w = (int)(q - row * g.W), W = g.W;
     const size_t base = row * W;
     const unsigned a = w > 0 ? __ldg(outMask + base + w - 1) : 0u, c = __ldg(outMask + base + w),
                    d = w + 1 < W ? __ldg(outMask + base + w + 1) : 0u;
     unsigned out[8];
-    if ((a | c | d) == 0u || c == 0xffffffffu) {  // no outside voxel within 32, or all outside
-#pragma unroll
-        for (int k = 0; k < 8; k++) out[k] = c ? 0u : 0xffffffffu;
-    } else {
-#pragma unroll
-        for (int j = 0; j < 8; j++) out[j] = ~nibble_bytes((c >> (4 * j)) & 0xfu);  // outside: 0, else none
-        unsigned cov = c;  // voxels with an outside voxel within k
-        for (int k = 1; k <= R; k++) {
-            // bit b of the right funnel shift is voxel b + k, of the left one voxel b - k
-            const unsigned nc = cov | __funnelshift_r(c, d, k) | __funnelshift_l(a, c, k);
-            const unsigned nw = nc & ~cov;  // nearest outside voxel at distance k
-            cov = nc;
-            if (nw == 0u) continue;
-            const unsigned v = (unsigned)(k * k) * 0x01010101u;
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const unsigned m = nibble_bytes((nw >> (4 * j)) & 0xfu);
-                out[j] = (out[j] & ~m) | (v & m);
-            }
-        }
-    }
+    z_word(a, c, d, g.R, out);
     uint4 *dst = reinterpret_cast<uint4 *>(zd + row * g.Gp + (size_t)w * 32);
     dst[0] = make_uint4(out[0], out[1], out[2], out[3]);
     dst[1] = make_uint4(out[4], out[5], out[6], out[7]);
@@ -577,7 +577,10 @@ static void launch_edt_shape(const QGrid &g, const unsigned *inMask, const unsig
 
 void launch_edt(const QGrid &g, const unsigned *inMask, const unsigned *outMask, unsigned char *codes,
                 unsigned *signMask, cudaStream_t s, int shape, unsigned char *zd) {
-    // zd (G G Gp bytes, optional): the z pass once per voxel, then tiles load it
+    // zd (G G Gp bytes, optional): the z pass once per voxel, then tiles load it.  Without
+    // it each tile computes its halo rows' z distances itself (the allocation-free entry
+    // point); with the bit-parallel z pass that measured the same or slower (0.846 against
+    // 0.836 ms on the 664^3 grid), so the pipeline keeps the separate pass.
     if (zd) {
         const size_t words = (size_t)g.G * g.G * g.W;
         k_edt_z<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(g, outMask, zd);
